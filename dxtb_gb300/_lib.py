@@ -1,0 +1,103 @@
+"""ctypes binding of ``libgbxtb.so`` (declarations in ``include/gbxtb.h``).
+
+The CUDA engine is the only implementation: if the library is missing the
+import fails loudly; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "libgbxtb.so"
+
+GBXTB_OK = 0
+MOL_OK = 0
+MOL_NOT_CONVERGED = 1
+MOL_FERMI_FAIL = 2
+MOL_CHOLESKY_FAIL = 4
+MOL_NONFINITE = 8
+
+EXPORTED = (
+    "gbxtb_version", "gbxtb_last_error", "gbxtb_ctx_create", "gbxtb_ctx_destroy",
+    "gbxtb_plan_create", "gbxtb_plan_destroy", "gbxtb_plan_sizes", "gbxtb_integrals",
+    "gbxtb_singlepoint", "gbxtb_get_status",
+)
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("max_z", C.c_int32),
+        ("n_shell_records", C.c_int32),
+        ("elem_shell0", C.POINTER(C.c_int32)),
+        ("elem_nshell", C.POINTER(C.c_int32)),
+        ("elem_data", C.POINTER(C.c_double)),
+        ("shell_int", C.POINTER(C.c_int32)),
+        ("shell_data", C.POINTER(C.c_double)),
+        ("kpair", C.POINTER(C.c_double)),
+        ("globals", C.POINTER(C.c_double)),
+    ]
+
+
+class Options(C.Structure):
+    _fields_ = [
+        ("maxiter", C.c_int32),
+        ("fermi_maxiter", C.c_int32),
+        ("broyden_memory", C.c_int32),
+        ("want_forces", C.c_int32),
+        ("x_atol", C.c_double),
+        ("x_atol_max", C.c_double),
+        ("kt", C.c_double),
+        ("broyden_alpha", C.c_double),
+    ]
+
+
+class GbxtbError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    """Load the engine library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise GbxtbError(
+            f"{LIB_PATH.name} is not built; run `python -m dxtb_gb300.build` "
+            "(the CUDA engine is required, there is no CPU fallback)"
+        )
+    lib = C.CDLL(str(LIB_PATH))
+    vp = C.c_void_p
+    lib.gbxtb_version.restype = C.c_int
+    lib.gbxtb_last_error.restype = C.c_char_p
+    lib.gbxtb_ctx_create.argtypes = [C.POINTER(Params), C.POINTER(vp)]
+    lib.gbxtb_ctx_destroy.argtypes = [vp]
+    lib.gbxtb_ctx_destroy.restype = None
+    lib.gbxtb_plan_create.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int64),
+                                      C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(vp),
+                                      C.POINTER(C.c_size_t)]
+    lib.gbxtb_plan_destroy.argtypes = [vp]
+    lib.gbxtb_plan_destroy.restype = None
+    lib.gbxtb_plan_sizes.argtypes = [vp, C.POINTER(C.c_int64)]
+    lib.gbxtb_integrals.argtypes = [vp, vp, vp, vp, vp, C.c_size_t, vp]
+    lib.gbxtb_singlepoint.argtypes = [vp, C.POINTER(Options), vp, vp, vp, vp, vp, C.c_size_t, vp]
+    lib.gbxtb_get_status.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+    for name in ("gbxtb_ctx_create", "gbxtb_plan_create", "gbxtb_plan_sizes", "gbxtb_integrals",
+                 "gbxtb_singlepoint", "gbxtb_get_status"):
+        getattr(lib, name).restype = C.c_int
+    _lib = lib
+    return lib
+
+
+def check(rc: int) -> None:
+    if rc != GBXTB_OK:
+        msg = load().gbxtb_last_error().decode(errors="replace")
+        raise GbxtbError(f"gbxtb error {rc}: {msg}")
+
+
+def ptr(a: np.ndarray, ctype):
+    return a.ctypes.data_as(C.POINTER(ctype))

@@ -1,0 +1,163 @@
+// Internal definitions shared by the gbxtb CUDA translation units.
+//
+// Data layout in HBM (ragged, no padding):
+//   * molecules m = 0..nmol-1 own contiguous ranges of atoms, shells and
+//     atomic orbitals (AOs); every per-molecule dense matrix (overlap S, core
+//     Hamiltonian H0, inverse Cholesky factor, Fock/eigenvector work arrays,
+//     density P) is a row-major nao x nao block at offset MolDesc::mat0 of a
+//     buffer that packs all molecules back to back;
+//   * the shell-resolved Coulomb matrix is an nsh x nsh block at MolDesc::gam0.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/gbxtb.h"
+
+namespace gbxtb {
+
+constexpr int kMaxPrim = GBXTB_MAX_PRIM;
+constexpr int kMaxL = 2;
+
+// molecule phases of the SCF state machine
+constexpr int kPhaseIterate = 0;  // mixing iterations
+constexpr int kPhaseFinal = 1;    // one more V -> Q pass with the unmixed potential
+constexpr int kPhaseDone = 2;
+
+struct MolDesc {
+  int32_t atom0, natom;
+  int32_t sh0, nsh;
+  int32_t ao0, nao;
+  int64_t mat0;   // offset of this molecule's nao*nao blocks
+  int64_t gam0;   // offset of its nsh*nsh block
+  int64_t pair0;  // first unordered shell pair (i <= j) of this molecule
+  double nel[2];  // alpha / beta electrons
+};
+
+// Parameter tables on the device.
+struct DevParams {
+  int max_z;
+  const int32_t *elem_shell0;
+  const int32_t *elem_nshell;
+  const double *elem_data;   // [z][GBXTB_ELEM_DOUBLES]
+  const int32_t *shell_int;  // [rec][GBXTB_SHELL_INTS]
+  const double *shell_data;  // [rec][GBXTB_SHELL_DOUBLES]
+  const double *kpair;       // [z][z]
+  double g[GBXTB_GLOBALS];
+};
+
+// Index maps of a planned batch (device arrays).
+struct DevPlan {
+  int nmol, natom, nsh, nao;
+  int64_t nmat, ngam, npair;
+  const MolDesc *mol;
+  const int32_t *atom_z, *atom_mol, *atom_sh0, *atom_nsh;
+  const int32_t *sh_atom, *sh_rec, *sh_ao, *sh_l, *sh_mol;  // sh_ao: AO offset inside the molecule
+  const int32_t *ao_sh;                                       // global shell of each AO
+  const double *ao_n0;                                        // reference occupation per AO
+};
+
+// Device scratch of one singlepoint call.
+struct Work {
+  // nao*nao blocks
+  double *S, *H0, *Linv, *A, *Z, *P;
+  double *invit;  // 5 * nmat: inverse-iteration LU factors
+  // per AO
+  double *eig, *d, *e, *tau, *occ, *q;  // occ: [2][nao_total]
+  // per shell
+  double *qsh, *vin, *vout, *vmix, *fprev, *xprev;  // potentials are shell resolved
+  double *hist_df, *hist_u;                          // [mem][nsh_total]
+  double *gam;                                       // nsh*nsh blocks
+  double *dedh;                                      // dE/dh per shell (forces)
+  // per atom
+  double *cn, *erep, *qat, *grad, *dedcn;  // grad: [natom][3]
+  // per molecule
+  int32_t *status, *phase, *iter, *kvec, *nhist;
+  double *efermi;   // [2][nmol]
+  double *energy;   // [nmol][6]: total, rep, h0, es2, es3, fermi
+  double *resid;    // [nmol][2]: L2, max norm of the last potential change
+  int32_t *active;  // [1]: molecules not yet done
+};
+
+// ---------------------------------------------------------------------------
+// device helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+__device__ __forceinline__ int warp_sum_int(int v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block-wide sum; `red` must hold at least blockDim.x/32 doubles.  All threads
+// get the result.
+__device__ __forceinline__ double block_sum(double v, double *red) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  double t = (threadIdx.x < nw) ? red[threadIdx.x] : 0.0;
+  if (wid == 0) t = warp_sum(t);
+  if (threadIdx.x == 0) red[0] = t;
+  __syncthreads();
+  double r = red[0];
+  __syncthreads();
+  return r;
+}
+
+__device__ __forceinline__ double block_max(double v, double *red) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  v = warp_max(v);
+  __syncthreads();
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  double t = (threadIdx.x < nw) ? red[threadIdx.x] : -1.0e308;
+  if (wid == 0) t = warp_max(t);
+  if (threadIdx.x == 0) red[0] = t;
+  __syncthreads();
+  double r = red[0];
+  __syncthreads();
+  return r;
+}
+
+__device__ __forceinline__ double block_min(double v, double *red) {
+  return -block_max(-v, red);
+}
+
+__device__ __forceinline__ bool mol_running(const Work &w, int m) {
+  return w.phase[m] != kPhaseDone;
+}
+
+// ---------------------------------------------------------------------------
+// host-side launch helpers (defined in the .cu files)
+// ---------------------------------------------------------------------------
+void launch_atoms(const DevParams &p, const DevPlan &pl, const Work &w, const double *pos,
+                  bool forces, cudaStream_t s);
+void launch_shellpairs(const DevParams &p, const DevPlan &pl, const Work &w, const double *pos,
+                       cudaStream_t s);
+void launch_cholesky(const DevPlan &pl, const Work &w, cudaStream_t s);
+void launch_fock(const DevPlan &pl, const Work &w, cudaStream_t s);
+void launch_eigensolve_tridiag(const DevPlan &pl, const Work &w, cudaStream_t s);
+void launch_fermi(const DevPlan &pl, const Work &w, double kt, int maxiter, cudaStream_t s);
+void launch_eigenvectors(const DevPlan &pl, const Work &w, cudaStream_t s);
+void launch_density(const DevPlan &pl, const Work &w, cudaStream_t s);
+void launch_charges_mix(const DevParams &p, const DevPlan &pl, const Work &w,
+                        const gbxtb_options &o, int iteration, cudaStream_t s);
+void launch_energies(const DevParams &p, const DevPlan &pl, const Work &w, double kt,
+                     double *energy_out, double *charges_out, cudaStream_t s);
+void launch_forces(const DevParams &p, const DevPlan &pl, const Work &w, const double *pos,
+                   double *grad_out, cudaStream_t s);
+
+}  // namespace gbxtb

@@ -1,0 +1,576 @@
+// Batched FP64 linear algebra of the SCF: generalised symmetric eigenproblem
+// F C = S C e for hundreds of molecules of different sizes.
+//
+// Reference behaviour reproduced: dxtb's diagonalize()
+// (scf/unrolling/base.py:141-175) calls tad_mctc's eighb, i.e. Cholesky
+// reduction S = L L^T, F' = L^-1 F L^-T, eigh(F'), C = L^-T U, eigenvalues
+// ascending; the density is P = C diag(f) C^T (scf/utils.py:29-52).
+//
+// GB300 design notes.  The FP64 pipe of a GB300 SM retires 2 DFMA per clock,
+// so an FP64 warp instruction occupies it for 16 cycles: every FP64 stage
+// here is written lane-parallel (no single-thread scalar chains):
+//   * Cholesky and L^-1: one block per molecule, columns of L^-1 per thread;
+//   * L^-1 F L^-T, C = L^-T Y, P = C f C^T and W = C (f e) C^T: one tiled
+//     FP64 GEMM kernel (64x64 tiles, 4x4 register micro-tiles) over a flat
+//     grid of (molecule, tile) pairs, skipping tiles outside triangular
+//     factors and computing symmetric products as lower tiles plus mirror;
+//   * tridiagonalisation: Householder, one block per molecule, warp-per-row
+//     symmetric matrix-vector products (coalesced rows);
+//   * eigenvalues: Sturm-sequence bisection, one thread per eigenvalue;
+//   * eigenvectors: inverse iteration on the tridiagonal matrix, one thread
+//     per cluster of close eigenvalues (modified Gram-Schmidt inside a
+//     cluster), only for orbitals with non-zero Fermi occupation;
+//   * back-transformation: each thread owns one eigenvector column and
+//     applies all Householder reflectors to it.
+#include "internal.cuh"
+
+#include <cmath>
+
+namespace gbxtb {
+
+namespace {
+
+constexpr double kEps = 2.220446049250313e-16;
+constexpr double kSafeMin = 2.2250738585072014e-308;
+
+__device__ __forceinline__ int find_mol_tile(const MolDesc *mol, const int64_t *tile0, int nmol,
+                                             int64_t t) {
+  int lo = 0, hi = nmol - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (tile0[mid] <= t) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// ---------------------------------------------------------------------------
+// Cholesky factorisation S = L L^T and L^-1 (lower triangular, zero upper)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(512) k_cholesky(DevPlan pl, Work w) {
+  const int m = blockIdx.x;
+  const MolDesc md = pl.mol[m];
+  const int n = md.nao;
+  double *L = w.A + md.mat0;      // work copy of S -> L
+  double *X = w.Linv + md.mat0;   // L^-1
+  const double *S = w.S + md.mat0;
+  __shared__ double diag;
+  __shared__ int fail;
+  if (threadIdx.x == 0) fail = 0;
+  for (int64_t e = threadIdx.x; e < (int64_t)n * n; e += blockDim.x) {
+    L[e] = S[e];
+    X[e] = 0.0;
+  }
+  __syncthreads();
+  for (int k = 0; k < n; ++k) {
+    if (threadIdx.x == 0) {
+      const double akk = L[(int64_t)k * n + k];
+      if (!(akk > 0.0)) {
+        fail = 1;
+        diag = 1.0;
+      } else {
+        diag = sqrt(akk);
+      }
+      L[(int64_t)k * n + k] = diag;
+    }
+    __syncthreads();
+    const double dk = diag;
+    for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) L[(int64_t)i * n + k] /= dk;
+    __syncthreads();
+    // trailing update of the lower triangle, warp per row
+    {
+      const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+      for (int i = k + 1 + wid; i < n; i += nw) {
+        const double lik = L[(int64_t)i * n + k];
+        for (int j = k + 1 + lane; j <= i; j += 32) L[(int64_t)i * n + j] -= lik * L[(int64_t)j * n + k];
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && fail) {
+    w.status[m] |= GBXTB_MOL_CHOLESKY_FAIL;
+    w.phase[m] = kPhaseDone;
+  }
+  // X = L^-1: thread owns column j, forward substitution down the column
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    X[(int64_t)j * n + j] = 1.0 / L[(int64_t)j * n + j];
+    for (int i = j + 1; i < n; ++i) {
+      double s = 0.0;
+      for (int k = j; k < i; ++k) s += L[(int64_t)i * n + k] * X[(int64_t)k * n + j];
+      X[(int64_t)i * n + j] = -s / L[(int64_t)i * n + i];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// batched FP64 GEMM
+//   mode 0: Z = Linv * F,  F = H0 - S o (v_i + v_j)/2 formed while loading
+//   mode 1: A = Z * Linv^T  (symmetric: lower tiles + mirror)
+//   mode 2: A = Linv^T * Y   (Y = Z, columns < kvec)
+//   mode 3: P = A diag(f) A^T  (f = occupation, K = kvec; symmetric)
+//   mode 4: Z = A diag(f e) A^T (energy-weighted density; symmetric)
+// ---------------------------------------------------------------------------
+constexpr int BM = 64, BN = 64, BK = 16;
+
+__global__ void __launch_bounds__(256) k_gemm(DevPlan pl, Work w, const int64_t *tile0, int mode, int all) {
+  const int64_t t = blockIdx.x;
+  const int m = find_mol_tile(pl.mol, tile0, pl.nmol, t);
+  if (!all && w.phase[m] == kPhaseDone) return;
+  const MolDesc md = pl.mol[m];
+  const int n = md.nao;
+  const int nt = (n + BN - 1) / BN;
+  const int local = (int)(t - tile0[m]);
+  const int ti = local / nt, tj = local % nt;
+  const int i0 = ti * BM, j0 = tj * BN;
+  const int kvec = min(max(w.kvec[m], 0), n);
+  const bool sym = (mode == 1 || mode == 3 || mode == 4);
+  const int ncol = (mode == 2) ? kvec : n;
+  const int K = (mode == 3 || mode == 4) ? kvec : n;
+  if (j0 >= ncol) return;
+  if (sym && j0 > i0) return;
+  int kmin = 0, kmax = K;
+  if (mode == 0) kmax = min(K, i0 + BM);
+  if (mode == 1) kmax = min(K, j0 + BN);
+  if (mode == 2) kmin = (i0 / BK) * BK;
+
+  const double *Lv = w.Linv + md.mat0;
+  const double *S = w.S + md.mat0, *H = w.H0 + md.mat0;
+  const double *Zs = w.Z + md.mat0, *As = w.A + md.mat0;
+  const double *occa = w.occ + md.ao0, *occb = w.occ + pl.nao + md.ao0;
+  const double *eig = w.eig + md.ao0;
+  const int32_t *aosh = pl.ao_sh + md.ao0;
+  const double *vin = w.vin;
+
+  __shared__ double sa[BK][BM + 1];
+  __shared__ double sb[BK][BN + 1];
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  double acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) acc[a][b] = 0.0;
+
+  for (int k0 = kmin; k0 < kmax; k0 += BK) {
+    // A tile: sa[kk][ii] = A(i0+ii, k0+kk)
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int e = tid + r * 256;
+      int ii, kk;
+      if (mode == 2) { kk = e >> 6; ii = e & 63; } else { ii = e >> 4; kk = e & 15; }
+      const int i = i0 + ii, k = k0 + kk;
+      double v = 0.0;
+      if (i < n && k < K) {
+        switch (mode) {
+          case 0: v = (k <= i) ? Lv[(int64_t)i * n + k] : 0.0; break;
+          case 1: v = Zs[(int64_t)i * n + k]; break;
+          case 2: v = (k >= i) ? Lv[(int64_t)k * n + i] : 0.0; break;
+          default: v = As[(int64_t)i * n + k]; break;
+        }
+      }
+      sa[kk][ii] = v;
+    }
+    // B tile: sb[kk][jj] = B(k0+kk, j0+jj)
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int e = tid + r * 256;
+      int jj, kk;
+      if (mode == 0 || mode == 2) { kk = e >> 6; jj = e & 63; } else { jj = e >> 4; kk = e & 15; }
+      const int j = j0 + jj, k = k0 + kk;
+      double v = 0.0;
+      if (j < ncol && k < K) {
+        switch (mode) {
+          case 0: {
+            const int64_t idx = (int64_t)k * n + j;
+            v = H[idx] - 0.5 * S[idx] * (vin[aosh[k]] + vin[aosh[j]]);
+            break;
+          }
+          case 1: v = (k <= j) ? Lv[(int64_t)j * n + k] : 0.0; break;
+          case 2: v = Zs[(int64_t)k * n + j]; break;
+          case 3: v = As[(int64_t)j * n + k] * (occa[k] + occb[k]); break;
+          default: v = As[(int64_t)j * n + k] * (occa[k] + occb[k]) * eig[k]; break;
+        }
+      }
+      sb[kk][jj] = v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      double a[4], b[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) a[r] = sa[kk][ty * 4 + r];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) b[c] = sb[kk][tx * 4 + c];
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[r][c] = fma(a[r], b[c], acc[r][c]);
+    }
+    __syncthreads();
+  }
+  double *C;
+  switch (mode) {
+    case 0: C = w.Z + md.mat0; break;
+    case 1: C = w.A + md.mat0; break;
+    case 2: C = w.A + md.mat0; break;
+    case 3: C = w.P + md.mat0; break;
+    default: C = w.Z + md.mat0; break;
+  }
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int i = i0 + ty * 4 + r;
+    if (i >= n) continue;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const int j = j0 + tx * 4 + c;
+      if (j >= ncol) continue;
+      if (sym) {
+        if (j > i) continue;
+        C[(int64_t)i * n + j] = acc[r][c];
+        C[(int64_t)j * n + i] = acc[r][c];
+      } else {
+        C[(int64_t)i * n + j] = acc[r][c];
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Householder tridiagonalisation of A (full symmetric storage, in place).
+// Reflector k (v with v_0 = 1) is stored in column k below the diagonal,
+// tau_k in w.tau, the tridiagonal in w.d / w.e.
+// ---------------------------------------------------------------------------
+constexpr int kTrdThreads = 512;
+
+__global__ void __launch_bounds__(kTrdThreads) k_tridiag(DevPlan pl, Work w) {
+  const int m = blockIdx.x;
+  if (w.phase[m] == kPhaseDone) return;
+  const MolDesc md = pl.mol[m];
+  const int n = md.nao;
+  double *A = w.A + md.mat0;
+  double *d = w.d + md.ao0, *e = w.e + md.ao0, *tau = w.tau + md.ao0;
+  extern __shared__ double sm[];
+  double *vs = sm;          // [n]
+  double *ps = sm + n;      // [n]
+  __shared__ double red[32];
+  __shared__ double sc[4];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int k = 0; k + 2 < n; ++k) {
+    const int m1 = n - k - 1;  // length of x
+    // column x = A[k+1.., k]
+    double part = 0.0;
+    for (int t = 1 + threadIdx.x; t < m1; t += blockDim.x) {
+      const double x = A[(int64_t)(k + 1 + t) * n + k];
+      part += x * x;
+    }
+    const double xn2 = block_sum(part, red);
+    if (threadIdx.x == 0) {
+      const double alpha = A[(int64_t)(k + 1) * n + k];
+      d[k] = A[(int64_t)k * n + k];
+      if (xn2 == 0.0) {
+        sc[0] = 0.0;      // tau
+        sc[1] = 0.0;      // scale
+        e[k] = alpha;
+      } else {
+        const double beta = -copysign(sqrt(alpha * alpha + xn2), alpha);
+        sc[0] = (beta - alpha) / beta;
+        sc[1] = 1.0 / (alpha - beta);
+        e[k] = beta;
+      }
+      tau[k] = sc[0];
+    }
+    __syncthreads();
+    const double tk = sc[0], scale = sc[1];
+    if (tk == 0.0) {
+      // no reflection needed: store a zero reflector
+      for (int t = threadIdx.x; t < m1; t += blockDim.x) A[(int64_t)(k + 1 + t) * n + k] = (t == 0) ? 1.0 : 0.0;
+      __syncthreads();
+      continue;
+    }
+    for (int t = threadIdx.x; t < m1; t += blockDim.x) {
+      double v = (t == 0) ? 1.0 : A[(int64_t)(k + 1 + t) * n + k] * scale;
+      vs[t] = v;
+      A[(int64_t)(k + 1 + t) * n + k] = v;
+    }
+    __syncthreads();
+    // p = tau * A22 v   (warp per row)
+    for (int i = wid; i < m1; i += nw) {
+      const double *row = A + (int64_t)(k + 1 + i) * n + (k + 1);
+      double s = 0.0;
+      for (int j = lane; j < m1; j += 32) s += row[j] * vs[j];
+      s = warp_sum(s);
+      if (lane == 0) ps[i] = tk * s;
+    }
+    __syncthreads();
+    double pv = 0.0;
+    for (int t = threadIdx.x; t < m1; t += blockDim.x) pv += ps[t] * vs[t];
+    const double K = block_sum(pv, red);
+    const double half = 0.5 * tk * K;
+    for (int t = threadIdx.x; t < m1; t += blockDim.x) ps[t] -= half * vs[t];  // w
+    __syncthreads();
+    // A22 -= v w^T + w v^T
+    for (int i = wid; i < m1; i += nw) {
+      double *row = A + (int64_t)(k + 1 + i) * n + (k + 1);
+      const double vi = vs[i], wi = ps[i];
+      for (int j = lane; j < m1; j += 32) row[j] -= vi * ps[j] + wi * vs[j];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    if (n >= 2) {
+      d[n - 2] = A[(int64_t)(n - 2) * n + (n - 2)];
+      d[n - 1] = A[(int64_t)(n - 1) * n + (n - 1)];
+      e[n - 2] = A[(int64_t)(n - 1) * n + (n - 2)];
+    } else {
+      d[0] = A[0];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// eigenvalues of the tridiagonal matrix by Sturm bisection
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_bisect(DevPlan pl, Work w) {
+  const int m = blockIdx.x;
+  if (w.phase[m] == kPhaseDone) return;
+  const MolDesc md = pl.mol[m];
+  const int n = md.nao;
+  extern __shared__ double sm[];
+  double *ds = sm, *e2 = sm + n;
+  __shared__ double red[32];
+  const double *d = w.d + md.ao0, *e = w.e + md.ao0;
+  double glo = 1e300, ghi = -1e300, emax = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    ds[i] = d[i];
+    const double el = (i > 0) ? fabs(e[i - 1]) : 0.0;
+    const double er = (i < n - 1) ? fabs(e[i]) : 0.0;
+    e2[i] = (i < n - 1) ? e[i] * e[i] : 0.0;
+    glo = fmin(glo, d[i] - el - er);
+    ghi = fmax(ghi, d[i] + el + er);
+    emax = fmax(emax, e2[i]);
+  }
+  glo = block_min(glo, red);
+  ghi = block_max(ghi, red);
+  emax = block_max(emax, red);
+  const double tnorm = fmax(fabs(glo), fabs(ghi));
+  glo -= 2.0 * kEps * tnorm * n + 1e-300;
+  ghi += 2.0 * kEps * tnorm * n + 1e-300;
+  const double pivmin = kSafeMin * fmax(1.0, emax);
+  for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
+    double lo = glo, hi = ghi;
+    for (int it = 0; it < 128; ++it) {
+      const double mid = 0.5 * (lo + hi);
+      if (mid <= lo || mid >= hi) break;
+      int cnt = 0;
+      double q = ds[0] - mid;
+      if (fabs(q) < pivmin) q = -pivmin;
+      cnt += (q < 0.0);
+      for (int j = 1; j < n; ++j) {
+        q = (ds[j] - mid) - e2[j - 1] / q;
+        if (fabs(q) < pivmin) q = -pivmin;
+        cnt += (q < 0.0);
+      }
+      if (cnt <= idx) lo = mid; else hi = mid;
+    }
+    w.eig[md.ao0 + idx] = 0.5 * (lo + hi);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// eigenvectors of the tridiagonal matrix by inverse iteration
+//   output Y[j][i] (component j of eigenvector i) in w.Z, i < kvec
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double start_value(int i, int j) {
+  const uint32_t h = (uint32_t)i * 2654435761u ^ ((uint32_t)j * 2246822519u + 0x9e3779b9u);
+  uint32_t x = h;
+  x ^= x >> 15; x *= 0x2c1b3c6du; x ^= x >> 12; x *= 0x297a2d39u; x ^= x >> 15;
+  return ((double)(x & 0xffffff) / 16777216.0) - 0.5;
+}
+
+__global__ void __launch_bounds__(128) k_invit(DevPlan pl, Work w) {
+  const int m = blockIdx.x;
+  if (w.phase[m] == kPhaseDone) return;
+  const MolDesc md = pl.mol[m];
+  const int n = md.nao;
+  const int kvec = min(max(w.kvec[m], 0), n);
+  const double *d = w.d + md.ao0, *e = w.e + md.ao0, *ev = w.eig + md.ao0;
+  double *Y = w.Z + md.mat0;
+  // scratch, interleaved by eigenvector index: X[j * n + i]
+  double *U1 = w.invit + md.mat0 * 5;
+  double *U2 = U1 + (int64_t)n * n;
+  double *U3 = U2 + (int64_t)n * n;
+  double *LM = U3 + (int64_t)n * n;
+  double *PV = LM + (int64_t)n * n;
+  __shared__ double red[32];
+  double tl = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double el = (i > 0) ? fabs(e[i - 1]) : 0.0;
+    const double er = (i < n - 1) ? fabs(e[i]) : 0.0;
+    tl = fmax(tl, fabs(d[i]) + el + er);
+  }
+  const double tnorm = block_max(tl, red);
+  const double ctol = 1e-3 * tnorm;
+  const double pert = kEps * tnorm;
+  for (int c = threadIdx.x; c < kvec; c += blockDim.x) {
+    if (c > 0 && ev[c] - ev[c - 1] <= ctol) continue;  // not a cluster start
+    int cend = c + 1;
+    while (cend < kvec && ev[cend] - ev[cend - 1] <= ctol) ++cend;
+    for (int i = c; i < cend; ++i) {
+      const double lam = ev[i];
+      // LU with partial pivoting of T - lam I: rows j: u1 diag, u2 super, u3 super2
+      double u1 = d[0] - lam;
+      double u2n = (n > 1) ? e[0] : 0.0;  // current super diagonal of row j
+      for (int j = 0; j < n - 1; ++j) {
+        const double sub = e[j];
+        const double dn = d[j + 1] - lam;
+        const double sup2 = (j + 1 < n - 1) ? e[j + 1] : 0.0;
+        if (fabs(u1) >= fabs(sub)) {
+          const double mult = (u1 != 0.0) ? sub / u1 : 0.0;
+          U1[(int64_t)j * n + i] = u1;
+          U2[(int64_t)j * n + i] = u2n;
+          U3[(int64_t)j * n + i] = 0.0;
+          LM[(int64_t)j * n + i] = mult;
+          PV[(int64_t)j * n + i] = 0.0;
+          u1 = dn - mult * u2n;
+          u2n = sup2;
+        } else {
+          const double mult = u1 / sub;
+          U1[(int64_t)j * n + i] = sub;
+          U2[(int64_t)j * n + i] = dn;
+          U3[(int64_t)j * n + i] = sup2;
+          LM[(int64_t)j * n + i] = mult;
+          PV[(int64_t)j * n + i] = 1.0;
+          u1 = u2n - mult * dn;
+          u2n = -mult * sup2;
+        }
+      }
+      U1[(int64_t)(n - 1) * n + i] = u1;
+      U2[(int64_t)(n - 1) * n + i] = 0.0;
+      U3[(int64_t)(n - 1) * n + i] = 0.0;
+      for (int j = 0; j < n; ++j) {
+        double u = U1[(int64_t)j * n + i];
+        if (fabs(u) < pert) U1[(int64_t)j * n + i] = (u < 0.0) ? -pert : pert;
+      }
+      // start vector
+      for (int j = 0; j < n; ++j) Y[(int64_t)j * n + i] = start_value(i, j);
+      for (int itr = 0; itr < 3; ++itr) {
+        // apply L^-1 (row interchanges)
+        for (int j = 0; j < n - 1; ++j) {
+          const double yj = Y[(int64_t)j * n + i], yj1 = Y[(int64_t)(j + 1) * n + i];
+          const double l = LM[(int64_t)j * n + i];
+          if (PV[(int64_t)j * n + i] != 0.0) {
+            Y[(int64_t)j * n + i] = yj1;
+            Y[(int64_t)(j + 1) * n + i] = yj - l * yj1;
+          } else {
+            Y[(int64_t)(j + 1) * n + i] = yj1 - l * yj;
+          }
+        }
+        // back substitution with U
+        double x1 = 0.0, x2 = 0.0;  // x[j+1], x[j+2]
+        double nrm = 0.0;
+        for (int j = n - 1; j >= 0; --j) {
+          double s = Y[(int64_t)j * n + i] - U2[(int64_t)j * n + i] * x1 - U3[(int64_t)j * n + i] * x2;
+          s /= U1[(int64_t)j * n + i];
+          Y[(int64_t)j * n + i] = s;
+          x2 = x1;
+          x1 = s;
+          nrm = fmax(nrm, fabs(s));
+        }
+        // rescale, then orthogonalise against earlier members of the cluster
+        const double inv = (nrm > 0.0) ? 1.0 / nrm : 1.0;
+        for (int j = 0; j < n; ++j) Y[(int64_t)j * n + i] *= inv;
+        for (int p = c; p < i; ++p) {
+          double dot = 0.0;
+          for (int j = 0; j < n; ++j) dot += Y[(int64_t)j * n + p] * Y[(int64_t)j * n + i];
+          for (int j = 0; j < n; ++j) Y[(int64_t)j * n + i] -= dot * Y[(int64_t)j * n + p];
+        }
+        double s2 = 0.0;
+        for (int j = 0; j < n; ++j) {
+          const double y = Y[(int64_t)j * n + i];
+          s2 += y * y;
+        }
+        const double in2 = 1.0 / sqrt(s2);
+        for (int j = 0; j < n; ++j) Y[(int64_t)j * n + i] *= in2;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// back-transformation Y <- Q Y, Q = H_0 ... H_{n-3}; thread per column
+// ---------------------------------------------------------------------------
+constexpr int kBtCols = 128;
+
+__global__ void __launch_bounds__(kBtCols) k_backtransform(DevPlan pl, Work w) {
+  const int m = blockIdx.y;
+  if (w.phase[m] == kPhaseDone) return;
+  const MolDesc md = pl.mol[m];
+  const int n = md.nao;
+  const int kvec = min(max(w.kvec[m], 0), n);
+  const int c0 = blockIdx.x * kBtCols;
+  if (c0 >= kvec) return;
+  const double *A = w.A + md.mat0;
+  const double *tau = w.tau + md.ao0;
+  double *Y = w.Z + md.mat0;
+  extern __shared__ double vsm[];
+  const int c = c0 + threadIdx.x;
+  for (int k = n - 3; k >= 0; --k) {
+    const int m1 = n - k - 1;
+    for (int t = threadIdx.x; t < m1; t += blockDim.x) vsm[t] = A[(int64_t)(k + 1 + t) * n + k];
+    __syncthreads();
+    const double tk = tau[k];
+    if (tk != 0.0 && c < kvec) {
+      double s = 0.0;
+      for (int r = 0; r < m1; ++r) s += vsm[r] * Y[(int64_t)(k + 1 + r) * n + c];
+      s *= tk;
+      for (int r = 0; r < m1; ++r) Y[(int64_t)(k + 1 + r) * n + c] -= s * vsm[r];
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+void launch_cholesky(const DevPlan &pl, const Work &w, cudaStream_t s) {
+  k_cholesky<<<pl.nmol, 512, 0, s>>>(pl, w);
+}
+
+void launch_gemm(const DevPlan &pl, const Work &w, const int64_t *tile0, int64_t ntile, int mode,
+                 int all, cudaStream_t s) {
+  if (ntile > 0) k_gemm<<<(unsigned)ntile, 256, 0, s>>>(pl, w, tile0, mode, all);
+}
+
+void launch_tridiag(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s) {
+  const size_t smem = sizeof(double) * 2 * (size_t)maxn;
+  k_tridiag<<<pl.nmol, kTrdThreads, smem, s>>>(pl, w);
+}
+
+void launch_bisect(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s) {
+  const size_t smem = sizeof(double) * 2 * (size_t)maxn;
+  k_bisect<<<pl.nmol, 256, smem, s>>>(pl, w);
+}
+
+void launch_invit(const DevPlan &pl, const Work &w, cudaStream_t s) {
+  k_invit<<<pl.nmol, 128, 0, s>>>(pl, w);
+}
+
+void launch_backtransform(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s) {
+  dim3 grid((maxn + kBtCols - 1) / kBtCols, pl.nmol);
+  k_backtransform<<<grid, kBtCols, sizeof(double) * (size_t)maxn, s>>>(pl, w);
+}
+
+cudaError_t set_linalg_smem_limits(int maxn) {
+  const size_t need = sizeof(double) * 2 * (size_t)maxn;
+  cudaError_t e = cudaSuccess;
+  if (need > 48 * 1024) {
+    e = cudaFuncSetAttribute(k_tridiag, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_bisect, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
+    if (e != cudaSuccess) return e;
+  }
+  return e;
+}
+
+}  // namespace gbxtb

@@ -1,0 +1,384 @@
+// SCF state update of GFN1-xTB on the device: Fermi-Dirac occupations,
+// Mulliken charges, ES2/ES3 potential, modified-Broyden mixing with the
+// reference's convergence test, and the energy assembly.
+//
+// Reference behaviour reproduced (dxtb, src/dxtb/_src/...):
+//   occupations   wavefunction/filling.py:201-366 (Newton on E_F from the
+//                 HOMO/LUMO midpoint, |sum f - n| <= sqrt(eps), exp cut at 50,
+//                 empty channels zero), called at scf/base.py:861-907
+//   charges       scf/base.py:764-815: q = n0 - diag(P S)
+//   potential     components/interactions/base.py:134-181,
+//                 coulomb/secondorder.py:415-442, coulomb/thirdorder.py:304-332
+//   convergence   scf/mixer/base.py:229-256 (L2 < x_atol and max < x_atol_max
+//                 on the change of the orbital potential) and
+//                 scf/unrolling/default.py:100-136 (the last unmixed output
+//                 potential defines the final charges)
+//   energies      scf/base.py:514-623 (E_H0 = tr(P H0), ES2 1/2 q gamma q,
+//                 ES3 gam3 q^3/3, electronic free energy kT sum f ln f +
+//                 (1-f) ln(1-f) over both spin channels with eps clamping),
+//                 calculators/types/energy.py:148-325 (total = classical + SCF)
+// The mixer is modified Broyden (Johnson, Phys. Rev. B 38, 12807 (1988)) on
+// the shell-resolved potential with orbital-multiplicity weights, so that all
+// norms and inner products equal those of the orbital-resolved vector the
+// reference mixes; the converged fixed point does not depend on the mixer.
+#include "internal.cuh"
+
+#include <cmath>
+
+namespace gbxtb {
+
+namespace {
+
+constexpr double kEps = 2.220446049250313e-16;
+
+// ---------------------------------------------------------------------------
+// Fermi occupations; also decides how many eigenvectors are needed (kvec).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_fermi(DevPlan pl, Work w, double kt, int maxiter) {
+  const int m = blockIdx.x;
+  if (w.phase[m] == kPhaseDone) return;
+  const MolDesc md = pl.mol[m];
+  const int n = md.nao;
+  const double *ev = w.eig + md.ao0;
+  double *occ[2] = {w.occ + md.ao0, w.occ + pl.nao + md.ao0};
+  __shared__ double red[32];
+  __shared__ int s_conv;
+  const double thr = sqrt(kEps);
+  double ef[2], target[2];
+  bool nonempty[2];
+  for (int s = 0; s < 2; ++s) {
+    const double nel = md.nel[s];
+    // index of the first orbital whose cumulative count reaches nel
+    int homo = 0;
+    while (homo < n - 1 && (double)(homo + 1) - nel < -5.0e-15) ++homo;
+    nonempty[s] = (nel != 0.0);
+    const int lumo = (n - 1 <= homo) ? homo : homo + 1;
+    ef[s] = nonempty[s] ? 0.5 * (ev[homo] + ev[lumo]) : 0.0;
+    target[s] = (double)homo + 1.0;
+  }
+  int it = 0;
+  for (; it < maxiter; ++it) {
+    double err[2];
+    for (int s = 0; s < 2; ++s) {
+      double sf = 0.0, sdf = 0.0;
+      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const double e = nonempty[s] ? ev[i] : 0.0;
+        const double x = (e - ef[s]) / kt;
+        double f, df;
+        if (x < 50.0) {
+          const double et = exp(x);
+          f = 1.0 / (et + 1.0);
+          df = et / (kt * (et + 1.0) * (et + 1.0));
+        } else {
+          f = 0.0;
+          df = kEps;
+        }
+        occ[s][i] = nonempty[s] ? f : 0.0;
+        sf += f;
+        sdf += df;
+      }
+      sf = block_sum(sf, red);
+      sdf = block_sum(sdf, red);
+      err[s] = target[s] - sf;
+      ef[s] += err[s] / sdf;
+    }
+    if (threadIdx.x == 0) s_conv = (fabs(err[0]) <= thr && fabs(err[1]) <= thr);
+    __syncthreads();
+    const int conv = s_conv;
+    __syncthreads();
+    if (conv) break;
+  }
+  if (threadIdx.x == 0) {
+    if (it >= maxiter) {
+      w.status[m] |= GBXTB_MOL_FERMI_FAIL;
+      w.phase[m] = kPhaseDone;
+    }
+    w.efermi[m] = ef[0];
+    w.efermi[pl.nmol + m] = ef[1];
+  }
+  __syncthreads();
+  // number of eigenvectors with non-zero occupation in either channel
+  int kmax = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x)
+    if (occ[0][i] > 0.0 || occ[1][i] > 0.0) kmax = max(kmax, i + 1);
+  const double km = block_max((double)kmax, red);
+  if (threadIdx.x == 0) w.kvec[m] = (int)km;
+}
+
+// ---------------------------------------------------------------------------
+// charges -> potential -> mixing (one block per molecule)
+// ---------------------------------------------------------------------------
+struct MixOpts {
+  double x_atol, x_atol_max, alpha, w0, kt;
+  int maxiter, memory, iteration;
+};
+
+__device__ __forceinline__ double wdot(const double *a, const double *b, const int32_t *l, int n) {
+  // orbital-multiplicity weighted dot product; caller reduces
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += (2.0 * l[i] + 1.0) * a[i] * b[i];
+  return s;
+}
+
+constexpr int kMixThreads = 256;
+constexpr int kMaxMem = 30;
+
+__global__ void __launch_bounds__(kMixThreads) k_charges_mix(DevParams p, DevPlan pl, Work w, MixOpts o) {
+  const int m = blockIdx.x;
+  const int phase = w.phase[m];
+  if (phase == kPhaseDone) return;
+  const MolDesc md = pl.mol[m];
+  const int n = md.nao, nsh = md.nsh, nat = md.natom;
+  const double *P = w.P + md.mat0, *S = w.S + md.mat0;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __shared__ double red[32];
+  __shared__ double a[kMaxMem][kMaxMem + 1];
+  __shared__ int s_flag;
+
+  // 1. orbital charges q = n0 - diag(P S)
+  for (int i = wid; i < n; i += nw) {
+    const double *pr = P + (int64_t)i * n, *sr = S + (int64_t)i * n;
+    double s = 0.0;
+    for (int j = lane; j < n; j += 32) s += pr[j] * sr[j];
+    s = warp_sum(s);
+    if (lane == 0) w.q[md.ao0 + i] = pl.ao_n0[md.ao0 + i] - s;
+  }
+  __syncthreads();
+  // 2. shell and atom charges
+  for (int i = threadIdx.x; i < nsh; i += blockDim.x) {
+    const int sh = md.sh0 + i;
+    const int o0 = pl.sh_ao[sh], no = 2 * pl.sh_l[sh] + 1;
+    double s = 0.0;
+    for (int k = 0; k < no; ++k) s += w.q[md.ao0 + o0 + k];
+    w.qsh[sh] = s;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nat; i += blockDim.x) {
+    const int at = md.atom0 + i;
+    double s = 0.0;
+    for (int k = 0; k < pl.atom_nsh[at]; ++k) s += w.qsh[pl.atom_sh0[at] + k];
+    w.qat[at] = s;
+  }
+  __syncthreads();
+  // 3. output potential v = gamma q_sh + gam3 q_at^2 (shell resolved)
+  const double *G = w.gam + md.gam0;
+  for (int i = wid; i < nsh; i += nw) {
+    double s = 0.0;
+    for (int j = lane; j < nsh; j += 32) s += G[(int64_t)i * nsh + j] * w.qsh[md.sh0 + j];
+    s = warp_sum(s);
+    if (lane == 0) {
+      const int sh = md.sh0 + i;
+      const int at = pl.sh_atom[sh];
+      const double g3 = p.elem_data[(size_t)pl.atom_z[at] * GBXTB_ELEM_DOUBLES + 1];
+      const double qa = w.qat[at];
+      w.vout[sh] = s + g3 * qa * qa;
+      w.vmix[sh] = s;  // ES2 part, kept for the energy
+    }
+  }
+  __syncthreads();
+
+  const int32_t *lsh = pl.sh_l + md.sh0;
+  double *vin = w.vin + md.sh0, *vout = w.vout + md.sh0;
+
+  if (phase == kPhaseFinal) {
+    // energies of the final state
+    double eh0 = 0.0;
+    const double *H = w.H0 + md.mat0;
+    for (int i = wid; i < n; i += nw) {
+      const double *pr = P + (int64_t)i * n, *hr = H + (int64_t)i * n;
+      double s = 0.0;
+      for (int j = lane; j < n; j += 32) s += pr[j] * hr[j];
+      eh0 += s;
+    }
+    eh0 = block_sum(eh0, red);
+    double es2 = 0.0;
+    for (int i = threadIdx.x; i < nsh; i += blockDim.x) es2 += 0.5 * w.qsh[md.sh0 + i] * w.vmix[md.sh0 + i];
+    es2 = block_sum(es2, red);
+    double es3 = 0.0, erep = 0.0;
+    for (int i = threadIdx.x; i < nat; i += blockDim.x) {
+      const int at = md.atom0 + i;
+      const double g3 = p.elem_data[(size_t)pl.atom_z[at] * GBXTB_ELEM_DOUBLES + 1];
+      const double qa = w.qat[at];
+      es3 += g3 * qa * qa * qa / 3.0;
+      erep += w.erep[at];
+    }
+    es3 = block_sum(es3, red);
+    erep = block_sum(erep, red);
+    double g = 0.0;
+    for (int s = 0; s < 2; ++s) {
+      const double *oc = w.occ + (size_t)s * pl.nao + md.ao0;
+      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const double f = fmax(oc[i], kEps), f1 = fmax(1.0 - oc[i], kEps);
+        g += f * log(f) + f1 * log(f1);
+      }
+    }
+    g = block_sum(g, red) * o.kt;
+    if (threadIdx.x == 0) {
+      double *en = w.energy + (size_t)m * 6;
+      en[1] = erep;
+      en[2] = eh0;
+      en[3] = es2;
+      en[4] = es3;
+      en[5] = g;
+      en[0] = erep + eh0 + es2 + es3 + g;
+      if (!isfinite(en[0])) w.status[m] |= GBXTB_MOL_NONFINITE;
+      w.phase[m] = kPhaseDone;
+    }
+    return;
+  }
+
+  // 4. convergence test on the change of the orbital potential
+  double l2 = 0.0, mx = 0.0;
+  for (int i = threadIdx.x; i < nsh; i += blockDim.x) {
+    const double f = vout[i] - vin[i];
+    l2 += (2.0 * lsh[i] + 1.0) * f * f;
+    mx = fmax(mx, fabs(f));
+  }
+  l2 = sqrt(block_sum(l2, red));
+  mx = block_max(mx, red);
+  const int iter = w.iter[m];
+  if (threadIdx.x == 0) {
+    w.resid[2 * m] = l2;
+    w.resid[2 * m + 1] = mx;
+    int flag = 0;
+    if (!isfinite(l2)) flag = 3;
+    else if (iter > 0 && l2 < o.x_atol && mx < o.x_atol_max) flag = 1;
+    else if (iter >= o.maxiter) flag = 2;
+    s_flag = flag;
+    if (flag == 3) {
+      w.status[m] |= GBXTB_MOL_NONFINITE;
+      w.phase[m] = kPhaseDone;
+    } else if (flag) {
+      if (flag == 2) w.status[m] |= GBXTB_MOL_NOT_CONVERGED;
+      w.phase[m] = kPhaseFinal;
+    }
+    w.iter[m] = iter + 1;
+  }
+  __syncthreads();
+  const int flag = s_flag;
+  if (flag == 3) return;
+  if (flag) {
+    for (int i = threadIdx.x; i < nsh; i += blockDim.x) vin[i] = vout[i];
+    return;
+  }
+
+  // 5. modified Broyden step
+  double *xprev = w.xprev + md.sh0, *fprev = w.fprev + md.sh0;
+  const int mem = o.memory;
+  const int nst = w.nhist[m];  // number of stored (dF, u) pairs ever pushed
+  if (iter == 0) {
+    for (int i = threadIdx.x; i < nsh; i += blockDim.x) {
+      const double f = vout[i] - vin[i];
+      xprev[i] = vin[i];
+      fprev[i] = f;
+      vin[i] = vin[i] + o.alpha * f;
+    }
+    return;
+  }
+  // new difference pair
+  double nrm = 0.0;
+  for (int i = threadIdx.x; i < nsh; i += blockDim.x) {
+    const double df = (vout[i] - vin[i]) - fprev[i];
+    nrm += (2.0 * lsh[i] + 1.0) * df * df;
+  }
+  nrm = sqrt(block_sum(nrm, red));
+  const double inrm = (nrm > 0.0) ? 1.0 / nrm : 0.0;
+  const int slot = nst % mem;
+  double *DF = w.hist_df + (size_t)slot * pl.nsh + md.sh0;
+  double *U = w.hist_u + (size_t)slot * pl.nsh + md.sh0;
+  for (int i = threadIdx.x; i < nsh; i += blockDim.x) {
+    const double f = vout[i] - vin[i];
+    const double df = (f - fprev[i]) * inrm;
+    DF[i] = df;
+    U[i] = o.alpha * df + (vin[i] - xprev[i]) * inrm;
+  }
+  __syncthreads();
+  const int k = min(nst + 1, mem);
+  // Gram matrix a_ij = <dF_i, dF_j> + w0^2 delta_ij and rhs c_i = <dF_i, F>
+  for (int pidx = wid; pidx < k * (k + 1); pidx += nw) {
+    const int ii = pidx / (k + 1), jj = pidx % (k + 1);
+    const double *x = w.hist_df + (size_t)ii * pl.nsh + md.sh0;
+    double s = 0.0;
+    if (jj < k) {
+      const double *y = w.hist_df + (size_t)jj * pl.nsh + md.sh0;
+      for (int t = lane; t < nsh; t += 32) s += (2.0 * lsh[t] + 1.0) * x[t] * y[t];
+    } else {
+      for (int t = lane; t < nsh; t += 32) s += (2.0 * lsh[t] + 1.0) * x[t] * (vout[t] - vin[t]);
+    }
+    s = warp_sum(s);
+    if (lane == 0) a[ii][jj] = s + ((ii == jj && jj < k) ? o.w0 * o.w0 : 0.0);
+  }
+  __syncthreads();
+  // Gauss-Jordan elimination (matrix is symmetric positive definite)
+  if (wid == 0) {
+    for (int piv = 0; piv < k; ++piv) {
+      const double inv = 1.0 / a[piv][piv];
+      __syncwarp();
+      for (int c = lane; c <= k; c += 32) a[piv][c] *= inv;
+      __syncwarp();
+      for (int r = 0; r < k; ++r) {
+        if (r == piv) continue;
+        const double fac = a[r][piv];
+        __syncwarp();
+        for (int c = lane; c <= k; c += 32) a[r][c] -= fac * a[piv][c];
+        __syncwarp();
+      }
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nsh; i += blockDim.x) {
+    const double f = vout[i] - vin[i];
+    double corr = 0.0;
+    for (int t = 0; t < k; ++t) corr += a[t][k] * w.hist_u[(size_t)t * pl.nsh + md.sh0 + i];
+    xprev[i] = vin[i];
+    fprev[i] = f;
+    vin[i] = vin[i] + o.alpha * f - corr;
+  }
+  if (threadIdx.x == 0) w.nhist[m] = nst + 1;
+}
+
+__global__ void k_count_active(DevPlan pl, Work w) {
+  __shared__ double red[32];
+  double c = 0.0;
+  for (int m = threadIdx.x; m < pl.nmol; m += blockDim.x) c += (w.phase[m] != kPhaseDone) ? 1.0 : 0.0;
+  c = block_sum(c, red);
+  if (threadIdx.x == 0) w.active[0] = (int)c;
+}
+
+__global__ void k_outputs(DevPlan pl, Work w, double *energy_out, double *charges_out) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < pl.nmol && energy_out) energy_out[t] = w.energy[t * 6];
+  if (t < pl.natom && charges_out) charges_out[t] = w.qat[t];
+}
+
+}  // namespace
+
+void launch_count_active(const DevPlan &pl, const Work &w, cudaStream_t s) {
+  k_count_active<<<1, 256, 0, s>>>(pl, w);
+}
+
+void launch_fermi(const DevPlan &pl, const Work &w, double kt, int maxiter, cudaStream_t s) {
+  k_fermi<<<pl.nmol, 128, 0, s>>>(pl, w, kt, maxiter);
+}
+
+void launch_charges_mix(const DevParams &p, const DevPlan &pl, const Work &w,
+                        const gbxtb_options &o, int iteration, cudaStream_t s) {
+  MixOpts mo;
+  mo.x_atol = o.x_atol;
+  mo.x_atol_max = o.x_atol_max;
+  mo.alpha = o.broyden_alpha;
+  mo.w0 = 0.01;
+  mo.kt = o.kt;
+  mo.maxiter = o.maxiter;
+  mo.memory = o.broyden_memory < 1 ? 1 : (o.broyden_memory > kMaxMem - 1 ? kMaxMem - 1 : o.broyden_memory);
+  mo.iteration = iteration;
+  k_charges_mix<<<pl.nmol, kMixThreads, 0, s>>>(p, pl, w, mo);
+}
+
+void launch_energies(const DevParams &, const DevPlan &pl, const Work &w, double,
+                     double *energy_out, double *charges_out, cudaStream_t s) {
+  const int64_t n = pl.nmol > pl.natom ? pl.nmol : pl.natom;
+  k_outputs<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(pl, w, energy_out, charges_out);
+}
+
+}  // namespace gbxtb

@@ -1,0 +1,145 @@
+/*
+ * gbxtb: GFN1-xTB single points (energy, charges, forces) on NVIDIA GB300.
+ *
+ * C ABI of libgbxtb.so.  All arrays named *_dev are device pointers owned by
+ * the caller; all other pointers are host memory.  Every entry point returns
+ * GBXTB_OK (0) or a negative error code and never aborts the process;
+ * gbxtb_last_error() gives a message for the last failure on this thread.
+ *
+ * The library replaces the reference calculator's single-point path
+ * (dxtb: src/dxtb/_src/calculators/types/energy.py:78-402 for the energy,
+ * src/dxtb/_src/calculators/types/autograd.py:82-201 and
+ * src/dxtb/_src/calculators/types/analytical.py:63-222 for the forces).
+ * A Python (ctypes) binding that mirrors dxtb's GFN1Calculator sits in
+ * dxtb_gb300/calculator.py; INTEGRATION.md shows the binding.
+ */
+#ifndef GBXTB_H
+#define GBXTB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBXTB_VERSION 1
+
+/* return codes */
+#define GBXTB_OK 0
+#define GBXTB_ERR_ARG (-1)      /* invalid argument (null pointer, bad size) */
+#define GBXTB_ERR_CUDA (-2)     /* a CUDA call failed */
+#define GBXTB_ERR_ELEMENT (-3)  /* atomic number without parameters */
+#define GBXTB_ERR_WORKSPACE (-4) /* workspace smaller than required */
+#define GBXTB_ERR_NOMEM (-5)    /* host or device allocation failed */
+
+/* per-molecule status bits (gbxtb_get_status) */
+#define GBXTB_MOL_OK 0
+#define GBXTB_MOL_NOT_CONVERGED 1 /* SCF hit maxiter; result is the last iterate,
+                                     as the reference returns with an
+                                     SCFConvergenceWarning
+                                     (scf/unrolling/default.py:123-136) */
+#define GBXTB_MOL_FERMI_FAIL 2    /* Fermi level not found in fermi_maxiter
+                                     (reference raises, wavefunction/filling.py:366) */
+#define GBXTB_MOL_CHOLESKY_FAIL 4 /* overlap not positive definite */
+#define GBXTB_MOL_NONFINITE 8     /* NaN/Inf appeared */
+
+typedef struct gbxtb_ctx gbxtb_ctx;
+typedef struct gbxtb_plan gbxtb_plan;
+
+/* Number of doubles per element / shell record in gbxtb_params. */
+#define GBXTB_ELEM_DOUBLES 8   /* gam, gam3, zeff, arep, en, rad(bohr), rcov_d3(bohr), 0 */
+#define GBXTB_SHELL_INTS 4     /* l, nprim, valence, 0 */
+#define GBXTB_SHELL_DOUBLES 24 /* alpha[8], coeff[8], level(Eh), kcn(Eh), shpoly, refocc, lgam, 0, 0, 0 */
+#define GBXTB_MAX_PRIM 8
+#define GBXTB_GLOBALS 16
+/* globals: 0 kpol, 1 enscale, 2 k_ss, 3 k_pp, 4 k_dd, 5 k_sp, 6 kexp (repulsion),
+ *          7 cn steepness, 8 cn cutoff, 9 repulsion cutoff, 10 integral cutoff,
+ *          11 gexp (must be 2), 12..15 unused */
+
+/* GFN1 parameter tables (host).  Element z uses shell records
+ * [elem_shell0[z], elem_shell0[z] + elem_nshell[z]).  Contraction
+ * coefficients already include primitive normalisation and the GFN1
+ * orthogonalisation of non-valence shells
+ * (dxtb: basis/bas.py:149-193, basis/slater.py:69-135, basis/ortho.py:74-110). */
+typedef struct {
+  int32_t max_z;              /* tables are indexed 0..max_z */
+  int32_t n_shell_records;
+  const int32_t *elem_shell0; /* [max_z+1] */
+  const int32_t *elem_nshell; /* [max_z+1], 0 = element not parametrised */
+  const double *elem_data;    /* [(max_z+1) * GBXTB_ELEM_DOUBLES] */
+  const int32_t *shell_int;   /* [n_shell_records * GBXTB_SHELL_INTS] */
+  const double *shell_data;   /* [n_shell_records * GBXTB_SHELL_DOUBLES] */
+  const double *kpair;        /* [(max_z+1) * (max_z+1)] */
+  const double *globals;      /* [GBXTB_GLOBALS] */
+} gbxtb_params;
+
+/* SCF options (dxtb: calculators/config/scf.py:32-433; defaults.py:130-260). */
+typedef struct {
+  int32_t maxiter;        /* SCF iterations (reference option "maxiter") */
+  int32_t fermi_maxiter;  /* Newton steps for the Fermi level (200) */
+  int32_t broyden_memory; /* mixer history length */
+  int32_t want_forces;    /* 0: energy only; 1: energy and forces */
+  double x_atol;          /* L2 norm of the potential change ("x_atol") */
+  double x_atol_max;      /* max norm of the potential change ("x_atol_max") */
+  double kt;              /* electronic temperature in Hartree (fermi_etemp * k_B) */
+  double broyden_alpha;   /* mixer step */
+} gbxtb_options;
+
+/* Library version (GBXTB_VERSION). */
+int gbxtb_version(void);
+
+/* Message describing the last error on the calling thread. */
+const char *gbxtb_last_error(void);
+
+/* Upload the parameter tables to the current CUDA device.
+ * Replaces dxtb's parameter loading (param/gfn1/load.py,
+ * calculators/types/base.py:451-734 constructor). */
+int gbxtb_ctx_create(const gbxtb_params *params, gbxtb_ctx **out);
+void gbxtb_ctx_destroy(gbxtb_ctx *ctx);
+
+/* Plan a batch of molecules: ragged atomic numbers (host), atom offsets
+ * (host, nmol+1), total charge and number of unpaired electrons per molecule
+ * (host; uhf may be NULL = derived from electron parity).  Builds the
+ * atom/shell/orbital maps on the host and uploads them (replaces
+ * basis/indexhelper.py:283-491 and scf/iterator.py:147-189).
+ * *workspace_bytes receives the device scratch size needed by
+ * gbxtb_singlepoint for this plan. */
+int gbxtb_plan_create(gbxtb_ctx *ctx, int32_t nmol, const int32_t *numbers,
+                      const int64_t *atom_offsets, const double *charge,
+                      const int32_t *uhf, gbxtb_plan **out,
+                      size_t *workspace_bytes);
+void gbxtb_plan_destroy(gbxtb_plan *plan);
+
+/* Sizes of a plan: [nmol, natoms, nshells, naos, nmat_doubles, nshellpair_doubles]. */
+int gbxtb_plan_sizes(const gbxtb_plan *plan, int64_t *sizes6);
+
+/* Overlap and core Hamiltonian for ragged positions (bohr, [natoms][3]).
+ * Outputs are per-molecule dense row-major nao x nao blocks, packed one after
+ * another (offset of molecule m = sum_{k<m} nao_k^2).
+ * Replaces integral/driver/pytorch/impls/overlap.py:147-243 and
+ * xtb/base.py:251-360. */
+int gbxtb_integrals(gbxtb_plan *plan, const double *positions_dev,
+                    double *overlap_dev, double *hcore_dev, void *workspace_dev,
+                    size_t workspace_bytes, void *stream);
+
+/* Full single point: energy per molecule, Mulliken atomic charges (nullable)
+ * and the energy gradient dE/dR ([natoms][3], nullable; required when
+ * opts->want_forces).  Replaces calculators/types/energy.py:78-402 (energy)
+ * and calculators/types/autograd.py:82-201 (forces = -gradient). */
+int gbxtb_singlepoint(gbxtb_plan *plan, const gbxtb_options *opts,
+                      const double *positions_dev, double *energy_dev,
+                      double *charges_dev, double *gradient_dev,
+                      void *workspace_dev, size_t workspace_bytes,
+                      void *stream);
+
+/* Per-molecule status bits and SCF iteration counts of the last
+ * gbxtb_singlepoint on this plan (host arrays of nmol). Synchronises the
+ * stream of that call. */
+int gbxtb_get_status(gbxtb_plan *plan, int32_t *status, int32_t *iterations);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBXTB_H */
