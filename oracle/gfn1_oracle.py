@@ -557,11 +557,51 @@ class Result:
     emo: np.ndarray | None = None
 
 
+class Broyden:
+    """Modified Broyden mixer (Johnson, Phys. Rev. B 38, 12807 (1988)) as run
+    by the GPU engine: step alpha, weights 1, w0 = 0.01, ``memory`` most
+    recent difference pairs."""
+
+    def __init__(self, alpha=0.3, memory=20, w0=0.01):
+        self.alpha, self.memory, self.w0 = alpha, memory, w0
+        self.df: list = []
+        self.u: list = []
+        self.xprev = None
+        self.fprev = None
+
+    def step(self, x, f):
+        if self.xprev is None:
+            self.xprev, self.fprev = x.copy(), f.copy()
+            return x + self.alpha * f
+        dfv = f - self.fprev
+        nrm = float(np.sqrt(dfv @ dfv))
+        inv = 1.0 / nrm if nrm > 0.0 else 0.0
+        self.df.append(dfv * inv)
+        self.u.append(self.alpha * dfv * inv + (x - self.xprev) * inv)
+        if len(self.df) > self.memory:
+            self.df.pop(0)
+            self.u.pop(0)
+        d = np.array(self.df)
+        a = d @ d.T + self.w0 ** 2 * np.eye(len(self.df))
+        gam = np.linalg.solve(a, d @ f)
+        self.xprev, self.fprev = x.copy(), f.copy()
+        return x + self.alpha * f - gam @ np.array(self.u)
+
+
 def singlepoint(numbers, positions, chrg: float = 0.0, spin=None, forces: bool = True,
                 etemp: float = 300.0, maxiter: int = 300, x_atol: float = 1e-10,
-                x_atol_max: float = 1e-10) -> Result:
-    """GFN1 single point without dispersion (calculators/types/energy.py:78-402,
-    scf/unrolling/default.py:71-136 for the single-system SCF loop)."""
+                x_atol_max: float = 1e-10, mixer: str = "anderson",
+                broyden_alpha: float = 0.3, broyden_memory: int = 20,
+                v_init: np.ndarray | None = None) -> Result:
+    """GFN1 single point without dispersion (calculators/types/energy.py:78-402).
+
+    ``mixer="anderson"`` replays the reference's single-system SCF loop
+    (scf/unrolling/default.py:71-136) step for step; ``mixer="broyden"``
+    replays the GPU engine's loop.  Both stop on the reference's test of the
+    potential change and take the final charges from the last unmixed
+    output potential, so both reach the same fixed point.  ``v_init``
+    (orbital-resolved potential) restarts the Broyden loop from a given
+    potential instead of zero, which checks that a state is a fixed point."""
     numbers = np.asarray(numbers, dtype=np.int64)
     positions = np.asarray(positions, dtype=np.float64)
     basis = Basis(numbers)
@@ -586,6 +626,8 @@ def singlepoint(numbers, positions, chrg: float = 0.0, spin=None, forces: bool =
     gam = gamma_matrix(basis, positions)
     gam3 = np.array([par["elements"][str(int(z))]["gam3"] for z in numbers])
     n0, nab = reference_occupation(basis, chrg, spin)
+    # Cholesky reduction of the generalised eigenproblem (scf/unrolling/base.py:141-175)
+    linv = scipy.linalg.solve_triangular(np.linalg.cholesky(smat), np.eye(basis.nao), lower=True)
 
     ao_sh, sh_atom = basis.ao_sh, basis.sh_atom
     nsh, nat = basis.nsh, len(numbers)
@@ -600,7 +642,9 @@ def singlepoint(numbers, positions, chrg: float = 0.0, spin=None, forces: bool =
 
     def pot_to_charges(v):
         f = h0 - 0.5 * smat * (v[:, None] + v[None, :])
-        emo, c = scipy.linalg.eigh(f, smat)
+        fp = linv @ f @ linv.T
+        emo, u = np.linalg.eigh(0.5 * (fp + fp.T))
+        c = linv.T @ u
         occ = fermi_occupation(emo, nab, kt)
         p = (c * occ.sum(0)) @ c.T
         q = n0 - np.einsum("ij,ji->i", p, smat)
@@ -613,18 +657,36 @@ def singlepoint(numbers, positions, chrg: float = 0.0, spin=None, forces: bool =
         vsh = gam @ qsh + (gam3 * qat * qat)[sh_atom]
         return vsh[ao_sh]
 
-    mixer = Anderson()
-    v_guess = np.zeros(basis.nao)
-    v_new = charges_to_pot(pot_to_charges(v_guess))
-    v = mixer.iter(v_new, v_guess)
     converged = False
     it = 0
-    for it in range(1, maxiter + 1):
-        v_new = charges_to_pot(pot_to_charges(v))
-        v = mixer.iter(v_new, v)
-        if mixer.converged(x_atol, x_atol_max):
-            converged = True
-            break
+    if mixer == "anderson":
+        mix = Anderson()
+        v_guess = np.zeros(basis.nao)
+        v_new = charges_to_pot(pot_to_charges(v_guess))
+        v = mix.iter(v_new, v_guess)
+        for it in range(1, maxiter + 1):
+            v_new = charges_to_pot(pot_to_charges(v))
+            v = mix.iter(v_new, v)
+            if mix.converged(x_atol, x_atol_max):
+                converged = True
+                break
+        it += 1
+    elif mixer == "broyden":
+        mix = Broyden(broyden_alpha, broyden_memory)
+        v = np.zeros(basis.nao) if v_init is None else np.asarray(v_init, dtype=np.float64).copy()
+        while True:
+            v_new = charges_to_pot(pot_to_charges(v))
+            f = v_new - v
+            if it > 0 and np.linalg.norm(f) < x_atol and np.max(np.abs(f)) < x_atol_max:
+                converged = True
+                break
+            if it >= maxiter:
+                break
+            v = mix.step(v, f)
+            it += 1
+        it += 1
+    else:
+        raise ValueError(f"unknown mixer {mixer!r}")
     # final charges from the unmixed last potential (scf/unrolling/default.py:111-114)
     q = pot_to_charges(v_new)
     p = state["p"]
@@ -640,7 +702,7 @@ def singlepoint(numbers, positions, chrg: float = 0.0, spin=None, forces: bool =
     res = Result(
         energy=float(eat.sum()), energy_atoms=eat, e_rep=float(erep_at.sum()),
         e_h0=float(e_h0.sum()), e_es2=float(e_es2.sum()), e_es3=float(e_es3.sum()),
-        e_fermi=g, charges=qat, iterations=it + 1, converged=converged, emo=state["emo"],
+        e_fermi=g, charges=qat, iterations=it, converged=converged, emo=state["emo"],
     )
     if forces:
         v_orb = charges_to_pot(q)

@@ -90,12 +90,17 @@ def singlepoint(numbers, positions, chrg: float = 0.0, spin=None, forces: bool =
     calc = dxtb.calculators.GFN1Calculator(num, opts=o, dtype=torch.float64)
     pos.requires_grad_(forces)
     res = calc.singlepoint(pos, chrg=chrg, spin=spin)
+    # the reference counts V -> Q -> V passes: the first one plus at most
+    # maxiter loop passes; reaching maxiter + 1 means it stopped unconverged
+    # (its OutputHandler records the SCFConvergenceWarning instead of raising)
+    converged = int(res.iter) <= int(o["maxiter"])
     total = res.total.sum(-1)
     out = {
         "energy": float(total.detach()),
         "scf": float(res.scf.sum(-1).detach()),
         "fenergy": float(res.fenergy.sum(-1).detach()),
         "iterations": int(res.iter),
+        "converged": converged,
         "charges_atom": calc.ihelp.reduce_orbital_to_atom(res.charges.mono).detach().numpy().copy(),
         "emo": res.emo.detach().numpy().copy(),
     }
