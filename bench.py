@@ -1,0 +1,378 @@
+#!/usr/bin/env python
+"""Benchmark: GFN1-xTB single points + forces per second on GB300 (FP64).
+
+Workload (per GPU): 512 seeded synthetic neutral CHNO molecules of 10-120
+atoms (30-360 basis functions), padded into one batch and solved in one
+engine call: integrals, SCF to |dv| < 1e-10 (L2 and max norm), energies and
+analytic forces.  A step is one such call.  With ``--gpus N`` (torchrun)
+every rank solves its own 512 molecules (weak scaling, no collective on the
+data path); ``value`` counts the molecules of all ranks.
+
+``--impl reference`` times the reference algorithm on the host cores: the
+numpy restatement of the reference's path (the reference itself is Python and
+its source tree is not available where the benchmark runs), in a process
+pool over all cores, on a bounded sample of the same molecules per step.
+
+Prints one JSON line (rank 0).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "single-points+forces/s (fp64, |dE|<=1e-8 Eh) batched vs plain on GB300; p50/p99"
+UNIT = "molecules/s"
+NMOL = 512
+OPTS = {"exclude": ["disp"], "maxiter": 300, "x_atol": 1e-10, "x_atol_max": 1e-10}
+CPU_SAMPLE = 48           # molecules in the host-core baseline sample
+REF_STEP_SAMPLE = 24      # molecules per step of the reference arm
+
+
+def workload_config(world: int) -> dict:
+    return {
+        "workload": "512 synthetic CHNO molecules per GPU, 10-120 atoms (uniform), energy + forces, "
+                    "SCF |dv|<1e-10, Fermi 300 K, D3 excluded",
+        "molecules_per_gpu": NMOL,
+        "global_batch": NMOL * world,
+        "atoms": "10-120",
+        "basis_functions": "30-360",
+        "parallelism": f"molecule shards x{world}" if world > 1 else "single GPU",
+        "l2": "inputs larger than L2 (workspace > 2 GB per call)",
+    }
+
+
+# ---------------------------------------------------------------------------
+# host-core legs (the oracle restatement of the reference algorithm)
+# ---------------------------------------------------------------------------
+def _cpu_one(args):
+    num, pos = args
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
+    from oracle import gfn1_oracle as go
+
+    r = go.singlepoint(num, pos, forces=True, mixer="anderson", maxiter=300)
+    return r.energy
+
+
+def cpu_throughput(mols, procs: int) -> tuple[float, float]:
+    import multiprocessing as mp
+
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(procs, initializer=_limit_threads) as pool:
+        pool.map(_cpu_one, mols[:procs][:2])  # warm the workers (imports)
+        t = time.perf_counter()
+        pool.map(_cpu_one, mols, chunksize=1)
+        dt = time.perf_counter() - t
+    return len(mols) / dt, dt
+
+
+def _limit_threads():
+    for k in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+        os.environ[k] = "1"
+    try:
+        from threadpoolctl import threadpool_limits
+
+        threadpool_limits(1)
+    except Exception:
+        pass
+
+
+# ---------------------------------------------------------------------------
+# GPU helpers
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.file, stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        self.file.flush()
+        rows = []
+        for line in Path(self.file.name).read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        smax = [num(r[2]) for r in rows if num(r[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": reasons, "samples": len(rows)}
+
+
+def flop_model(plan_n: np.ndarray, kocc: np.ndarray, iters: np.ndarray) -> dict:
+    """Algorithmic FP64 flops per kernel class for the whole call (LAPACK
+    counts): tridiagonalisation 4/3 N^3, L^-1 F L^-T 4/3 N^3, density
+    (C = L^-T Y and P = C f C^T) 2 N^2 k, back-transformation 2 N^2 k per SCF
+    pass; k = occupied orbitals."""
+    n = plan_n.astype(np.float64)
+    k = kocc.astype(np.float64)
+    passes = iters.astype(np.float64)
+    return {
+        "tridiag": float(np.sum(passes * 4.0 / 3.0 * n ** 3)),
+        "fock": float(np.sum(passes * 4.0 / 3.0 * n ** 3)),
+        "density": float(np.sum(passes * 2.0 * n * n * k)),
+        "backtransform": float(np.sum(passes * 2.0 * n * n * k)),
+        "cholesky": float(np.sum(2.0 / 3.0 * n ** 3)),
+    }
+
+
+def molecule_dims(mols):
+    from dxtb_gb300 import params
+
+    raw = params.raw()["elements"]
+    n = np.array([sum(2 * s["l"] + 1 for z in num for s in raw[str(int(z))]["shells"]) for num, _ in mols])
+    nel = np.array([params.reference_electrons(num) for num, _ in mols])
+    return n, np.ceil(nel / 2.0)
+
+
+def pad(mols):
+    nmax = max(len(m[0]) for m in mols)
+    num = np.zeros((len(mols), nmax), dtype=np.int64)
+    pos = np.zeros((len(mols), nmax, 3))
+    for i, (a, b) in enumerate(mols):
+        num[i, :len(a)] = a
+        pos[i, :len(a)] = b
+    return num, pos
+
+
+# ---------------------------------------------------------------------------
+def run_reference_arm(args, rank: int, world: int) -> None:
+    if rank != 0:
+        return
+    from dxtb_gb300 import molgen
+
+    procs = os.cpu_count() or 1
+    mols = molgen.c2_batch(NMOL)
+    step_vals = []
+    n_total = args.warmup + args.steps
+    for s in range(n_total):
+        lo = (s * REF_STEP_SAMPLE) % NMOL
+        sample = mols[lo:lo + REF_STEP_SAMPLE]
+        v, dt = cpu_throughput(sample, procs)
+        if s >= args.warmup:
+            step_vals.append((v, dt))
+    total_mols = REF_STEP_SAMPLE * len(step_vals)
+    total_t = sum(dt for _, dt in step_vals)
+    value = total_mols / total_t
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_t / len(step_vals),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded CHNO molecules)", "config": workload_config(1),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port",
+                         "sample": f"{REF_STEP_SAMPLE} molecules per step (consecutive slices of the 512), "
+                                   "numpy restatement of the reference path incl. its Anderson mixer, "
+                                   "one process per core"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gbxtb", choices=["gbxtb", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        run_reference_arm(args, rank, world)
+        return
+
+    from dxtb_gb300 import molgen
+
+    mols = molgen.c2_batch(NMOL, shard=rank)
+
+    # host-core baseline first (spawned workers, before any CUDA call)
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        procs = os.cpu_count() or 1
+        v, dt = cpu_throughput(mols[:CPU_SAMPLE], procs)
+        cpu = {"value": v, "unit": UNIT, "cores": procs, "kind": "port",
+               "sample": f"first {CPU_SAMPLE} of the 512 molecules, energy + forces, numpy restatement of "
+                         f"the reference path incl. its Anderson mixer, one process per core ({dt:.1f} s)"}
+
+    import torch
+    import torch.distributed as dist
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=dev)
+
+    from dxtb_gb300 import GFN1Calculator, _lib
+
+    num, pos = pad(mols)
+    calc = GFN1Calculator(torch.as_tensor(num), opts={**OPTS, "profile": True})
+    pos_dev = torch.tensor(pos, device=dev)
+    pos_host = torch.tensor(pos).pin_memory()
+    import warnings
+
+    warnings.simplefilter("ignore")
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    def max_over_ranks(x: float) -> float:
+        if world == 1:
+            return x
+        t = torch.tensor([x], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # warm-up
+    for _ in range(args.warmup):
+        res = calc.singlepoint(pos_dev, forces=True)
+    torch.cuda.synchronize()
+
+    # device-resident timing (value)
+    prof_ms: dict = {}
+    launches = 0
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        for _ in range(args.steps):
+            res = calc.singlepoint(pos_dev, forces=True)
+            for k, v in calc.last_profile["ms"].items():
+                prof_ms[k] = prof_ms.get(k, 0.0) + v
+            launches += calc.last_profile["total_launches"]
+        ev1.record()
+        torch.cuda.synchronize()
+    barrier()
+    t_dev = max_over_ranks(ev0.elapsed_time(ev1) / 1e3)
+    value = NMOL * world * args.steps / t_dev
+
+    # end to end through the public API with host buffers
+    nbytes_in = pos_host.numel() * 8
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        p = pos_host.to(dev, non_blocking=True)
+        r = calc.singlepoint(p, forces=True)
+        e_host = r.energy.cpu()
+        f_host = r.gradient.cpu()
+    torch.cuda.synchronize()
+    barrier()
+    t_e2e = max_over_ranks(time.perf_counter() - t0)
+    nbytes_out = e_host.numel() * 8 + f_host.numel() * 8
+    e2e = NMOL * world * args.steps / t_e2e
+
+    # parity summary of this run against the reference's own results (rank 0 set)
+    parity = None
+    ref_path = ROOT / "tests" / "golden" / "workload_batch_ref.npz"
+    if rank == 0 and ref_path.exists():
+        ref = np.load(ref_path)
+        e = res.energy.cpu().numpy()
+        ok = (res.status == 0) & ref["converged"]
+        d = np.abs(e - ref["energy"])
+        same = ok & (d < 1e-5)
+        parity = {"molecules": NMOL, "engine_converged": int((res.status == 0).sum()),
+                  "reference_converged": int(ref["converged"].sum()),
+                  "same_scf_state": int(same.sum()),
+                  "within_1e-8": int((same & (d <= 1e-8)).sum()),
+                  "max_dE_same_state": float(d[same].max()) if same.any() else None,
+                  "iterations_mean": float(res.iterations.mean()),
+                  "iterations_max": int(res.iterations.max())}
+
+    # roofline of the dominant kernel class
+    n, kocc = molecule_dims(mols)
+    fl = flop_model(n, kocc, res.iterations + 1)
+    per_step_ms = {k: v / args.steps for k, v in prof_ms.items()}
+    dominant = max(per_step_ms, key=per_step_ms.get)
+    lib = _lib.load()
+    import ctypes as C
+
+    g = C.c_double()
+    _lib.check(lib.gbxtb_fp64_peak(C.byref(g)))
+    fp64_peak = g.value / 1e3  # TFLOP/s
+    roof = None
+    if dominant in fl and per_step_ms[dominant] > 0:
+        achieved = fl[dominant] / (per_step_ms[dominant] * 1e-3) / 1e12
+        roof = {"bound": "fp64", "kernel": dominant, "achieved": achieved, "peak": fp64_peak,
+                "unit": "TFLOP/s", "frac": achieved / fp64_peak, "traffic": None,
+                "peak_source": "measured FP64 FMA microbenchmark (gbxtb_fp64_peak) in this run"}
+    else:
+        roof = {"bound": "fp64", "kernel": dominant, "achieved": None, "peak": fp64_peak,
+                "unit": "TFLOP/s", "frac": None, "traffic": None,
+                "peak_source": "measured FP64 FMA microbenchmark (gbxtb_fp64_peak) in this run"}
+
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded CHNO molecules)", "config": workload_config(world),
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(nbytes_in),
+                    "d2h_bytes_per_step": int(nbytes_out)},
+            "gpu_launches": int(launches),
+            "clocks": clk.summary(),
+            "roofline": roof,
+            "stage_ms_per_step": {k: round(v, 3) for k, v in per_step_ms.items()},
+            "parity": parity,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -22,8 +22,12 @@ MOL_NONFINITE = 8
 EXPORTED = (
     "gbxtb_version", "gbxtb_last_error", "gbxtb_ctx_create", "gbxtb_ctx_destroy",
     "gbxtb_plan_create", "gbxtb_plan_destroy", "gbxtb_plan_sizes", "gbxtb_integrals",
-    "gbxtb_singlepoint", "gbxtb_get_status",
+    "gbxtb_singlepoint", "gbxtb_get_status", "gbxtb_get_shell_potential", "gbxtb_get_profile",
+    "gbxtb_fp64_peak",
 )
+
+PROF_CLASSES = ("atoms", "shellpairs", "cholesky", "fock", "tridiag", "bisect", "fermi", "invit",
+                "backtransform", "density", "mix", "forces")
 
 
 class Params(C.Structure):
@@ -50,6 +54,8 @@ class Options(C.Structure):
         ("x_atol_max", C.c_double),
         ("kt", C.c_double),
         ("broyden_alpha", C.c_double),
+        ("profile", C.c_int32),
+        ("reserved", C.c_int32),
     ]
 
 
@@ -86,8 +92,12 @@ def load() -> C.CDLL:
     lib.gbxtb_integrals.argtypes = [vp, vp, vp, vp, vp, C.c_size_t, vp]
     lib.gbxtb_singlepoint.argtypes = [vp, C.POINTER(Options), vp, vp, vp, vp, vp, C.c_size_t, vp]
     lib.gbxtb_get_status.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+    lib.gbxtb_get_shell_potential.argtypes = [vp, C.POINTER(C.c_double)]
+    lib.gbxtb_fp64_peak.argtypes = [C.POINTER(C.c_double)]
+    lib.gbxtb_fp64_peak.restype = C.c_int
+    lib.gbxtb_get_profile.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     for name in ("gbxtb_ctx_create", "gbxtb_plan_create", "gbxtb_plan_sizes", "gbxtb_integrals",
-                 "gbxtb_singlepoint", "gbxtb_get_status"):
+                 "gbxtb_singlepoint", "gbxtb_get_status", "gbxtb_get_shell_potential", "gbxtb_get_profile"):
         getattr(lib, name).restype = C.c_int
     _lib = lib
     return lib

@@ -19,7 +19,7 @@ BUILD = PKG / "_build"
 LIB = PKG / "libgbxtb.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
     "-Xcompiler", "-Wall", "-I", str(PKG.parent / "include")]
 
 

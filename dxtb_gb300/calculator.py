@@ -55,6 +55,7 @@ DEFAULT_OPTS = {
     "broyden_alpha": 0.3,
     "broyden_memory": 20,
     "verbosity": 0,
+    "profile": False,        # per-stage device timings (last_profile)
 }
 _ACCEPTED_IGNORED = {"scf_mode", "scp_mode", "int_driver", "int_level", "batch_mode", "damp",
                      "damp_init", "mix_guess", "cache_enabled", "timer", "strict", "log_level"}
@@ -67,6 +68,7 @@ class Result:
     gradient: torch.Tensor | None  # ragged dE/dR
     status: np.ndarray
     iterations: np.ndarray
+    shell_potential: np.ndarray | None = None  # final shell-resolved potential (host)
 
 
 class _Context:
@@ -208,6 +210,7 @@ class GFN1Calculator:
         self._ctx = _Context.get(self.device.index)
         self._plans: dict = {}
         self._cache: dict = {}
+        self.last_profile: dict = {}
 
     # ------------------------------------------------------------------ layout
     def _ragged_positions(self, positions: torch.Tensor) -> torch.Tensor:
@@ -260,6 +263,7 @@ class GFN1Calculator:
         opt.x_atol_max = float(o["x_atol_max"])
         opt.kt = float(o["fermi_etemp"]) * params.KELVIN2AU
         opt.broyden_alpha = float(o["broyden_alpha"])
+        opt.profile = 1 if o["profile"] else 0
         return opt
 
     def _run(self, positions: torch.Tensor, chrg=0, spin=None, forces: bool = False) -> Result:
@@ -280,8 +284,19 @@ class GFN1Calculator:
         status = np.zeros(plan.nmol, dtype=np.int32)
         iters = np.zeros(plan.nmol, dtype=np.int32)
         _lib.check(lib.gbxtb_get_status(plan.handle, _lib.ptr(status, C.c_int32), _lib.ptr(iters, C.c_int32)))
+        vsh = np.zeros(int(plan.sizes[2]), dtype=np.float64)
+        _lib.check(lib.gbxtb_get_shell_potential(plan.handle, _lib.ptr(vsh, C.c_double)))
+        ms = np.zeros(len(_lib.PROF_CLASSES), dtype=np.float64)
+        nl = np.zeros(len(_lib.PROF_CLASSES), dtype=np.int64)
+        tot = C.c_int64()
+        _lib.check(lib.gbxtb_get_profile(plan.handle, _lib.ptr(ms, C.c_double), _lib.ptr(nl, C.c_int64),
+                                         C.byref(tot)))
+        self.last_profile = {"ms": dict(zip(_lib.PROF_CLASSES, ms.tolist())),
+                             "launches": dict(zip(_lib.PROF_CLASSES, nl.tolist())),
+                             "total_launches": int(tot.value)}
         self._raise_on_status(status)
-        return Result(energy=energy, charges=charges, gradient=grad, status=status, iterations=iters)
+        return Result(energy=energy, charges=charges, gradient=grad, status=status, iterations=iters,
+                      shell_potential=vsh)
 
     def _raise_on_status(self, status: np.ndarray) -> None:
         if (status & _lib.MOL_FERMI_FAIL).any():

@@ -80,6 +80,12 @@ struct gbxtb_plan {
   Work last_work{};
   bool has_run = false;
   int32_t *h_active = nullptr;  // pinned
+  // profiling
+  cudaEvent_t ev[GBXTB_PROF_CLASSES][2] = {};
+  bool ev_ready = false;
+  double prof_ms[GBXTB_PROF_CLASSES] = {};
+  int64_t prof_launches[GBXTB_PROF_CLASSES] = {};
+  int64_t total_launches = 0;
 };
 
 namespace {
@@ -377,6 +383,9 @@ int gbxtb_plan_create(gbxtb_ctx *ctx, int32_t nmol, const int32_t *numbers,
 
 void gbxtb_plan_destroy(gbxtb_plan *plan) {
   if (!plan) return;
+  if (plan->ev_ready)
+    for (int c = 0; c < GBXTB_PROF_CLASSES; ++c)
+      for (int k = 0; k < 2; ++k) cudaEventDestroy(plan->ev[c][k]);
   if (plan->dbuf) cudaFree(plan->dbuf);
   if (plan->h_active) cudaFreeHost(plan->h_active);
   delete plan;
@@ -417,6 +426,38 @@ int gbxtb_integrals(gbxtb_plan *plan, const double *positions_dev, double *overl
   return GBXTB_OK;
 }
 
+namespace {
+// Stream-ordered timing of kernel classes: begin/end record events; the
+// elapsed times are harvested after each host synchronisation.
+struct Prof {
+  gbxtb_plan *pl;
+  cudaStream_t s;
+  bool on;
+  bool pending[GBXTB_PROF_CLASSES] = {};
+  void begin(int c) {
+    if (on) cudaEventRecord(pl->ev[c][0], s);
+  }
+  void end(int c, int launches) {
+    pl->total_launches += launches;
+    pl->prof_launches[c] += launches;
+    if (on) {
+      cudaEventRecord(pl->ev[c][1], s);
+      pending[c] = true;
+    }
+  }
+  // after a stream synchronisation
+  void harvest() {
+    if (!on) return;
+    for (int c = 0; c < GBXTB_PROF_CLASSES; ++c)
+      if (pending[c]) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, pl->ev[c][0], pl->ev[c][1]) == cudaSuccess) pl->prof_ms[c] += ms;
+        pending[c] = false;
+      }
+  }
+};
+}  // namespace
+
 int gbxtb_singlepoint(gbxtb_plan *plan, const gbxtb_options *opts, const double *positions_dev,
                       double *energy_dev, double *charges_dev, double *gradient_dev,
                       void *workspace_dev, size_t workspace_bytes, void *stream) {
@@ -431,6 +472,17 @@ int gbxtb_singlepoint(gbxtb_plan *plan, const gbxtb_options *opts, const double 
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const DevPlan &pl = plan->pl;
   const DevParams &p = plan->ctx->p;
+  if (opts->profile && !plan->ev_ready) {
+    for (int c = 0; c < GBXTB_PROF_CLASSES; ++c)
+      for (int k = 0; k < 2; ++k) CK(cudaEventCreate(&plan->ev[c][k]));
+    plan->ev_ready = true;
+  }
+  for (int c = 0; c < GBXTB_PROF_CLASSES; ++c) {
+    plan->prof_ms[c] = 0.0;
+    plan->prof_launches[c] = 0;
+  }
+  plan->total_launches = 0;
+  Prof pf{plan, s, opts->profile != 0};
   // reset state
   CK(cudaMemsetAsync(w.status, 0, sizeof(int32_t) * pl.nmol, s));
   CK(cudaMemsetAsync(w.phase, 0, sizeof(int32_t) * pl.nmol, s));
@@ -440,35 +492,65 @@ int gbxtb_singlepoint(gbxtb_plan *plan, const gbxtb_options *opts, const double 
   CK(cudaMemsetAsync(w.vin, 0, sizeof(double) * pl.nsh, s));
   CK(cudaMemsetAsync(w.energy, 0, sizeof(double) * 6 * pl.nmol, s));
   // geometry-dependent terms
+  pf.begin(GBXTB_PROF_ATOMS);
   launch_atoms(p, pl, w, positions_dev, opts->want_forces != 0, s);
+  pf.end(GBXTB_PROF_ATOMS, 1);
+  pf.begin(GBXTB_PROF_SHELLPAIRS);
   launch_shellpairs(p, pl, w, positions_dev, s);
+  pf.end(GBXTB_PROF_SHELLPAIRS, 1);
+  pf.begin(GBXTB_PROF_CHOLESKY);
   launch_cholesky(pl, w, s);
+  pf.end(GBXTB_PROF_CHOLESKY, 1);
   CK(cudaGetLastError());
   // SCF: maxiter mixing iterations + the first evaluation + the final pass
   const int max_loops = opts->maxiter + 3;
   for (int it = 0; it < max_loops; ++it) {
+    pf.begin(GBXTB_PROF_FOCK);
     launch_gemm(pl, w, plan->tile0, plan->ntile, 0, 0, s);
     launch_gemm(pl, w, plan->tile0, plan->ntile, 1, 0, s);
+    pf.end(GBXTB_PROF_FOCK, 2);
+    pf.begin(GBXTB_PROF_TRIDIAG);
     launch_tridiag(pl, w, plan->maxn, s);
+    pf.end(GBXTB_PROF_TRIDIAG, 1);
+    pf.begin(GBXTB_PROF_BISECT);
     launch_bisect(pl, w, plan->maxn, s);
+    pf.end(GBXTB_PROF_BISECT, 1);
+    pf.begin(GBXTB_PROF_FERMI);
     launch_fermi(pl, w, opts->kt, opts->fermi_maxiter, s);
+    pf.end(GBXTB_PROF_FERMI, 1);
+    pf.begin(GBXTB_PROF_INVIT);
     launch_invit(pl, w, s);
+    pf.end(GBXTB_PROF_INVIT, 1);
+    pf.begin(GBXTB_PROF_BACKTRANSFORM);
     launch_backtransform(pl, w, plan->maxn, s);
+    pf.end(GBXTB_PROF_BACKTRANSFORM, 1);
+    pf.begin(GBXTB_PROF_DENSITY);
     launch_gemm(pl, w, plan->tile0, plan->ntile, 2, 0, s);
     launch_gemm(pl, w, plan->tile0, plan->ntile, 3, 0, s);
+    pf.end(GBXTB_PROF_DENSITY, 2);
+    pf.begin(GBXTB_PROF_MIX);
     launch_charges_mix(p, pl, w, *opts, it, s);
     launch_count_active(pl, w, s);
+    pf.end(GBXTB_PROF_MIX, 2);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(plan->h_active, w.active, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
+    pf.harvest();
     if (plan->h_active[0] == 0) break;
   }
   launch_energies(p, pl, w, opts->kt, energy_dev, charges_dev, s);
+  plan->total_launches += 1;
   if (opts->want_forces) {
+    pf.begin(GBXTB_PROF_FORCES);
     launch_gemm(pl, w, plan->tile0, plan->ntile, 4, 1, s);
     launch_forces(p, pl, w, positions_dev, gradient_dev, s);
+    pf.end(GBXTB_PROF_FORCES, 3);
   }
   CK(cudaGetLastError());
+  if (pf.on) {
+    CK(cudaStreamSynchronize(s));
+    pf.harvest();
+  }
   plan->last_stream = s;
   plan->last_work = w;
   plan->has_run = true;
@@ -481,6 +563,24 @@ int gbxtb_get_status(gbxtb_plan *plan, int32_t *status, int32_t *iterations) {
   const int n = plan->pl.nmol;
   if (status) CK(cudaMemcpy(status, plan->last_work.status, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
   if (iterations) CK(cudaMemcpy(iterations, plan->last_work.iter, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+  return GBXTB_OK;
+}
+
+int gbxtb_get_profile(gbxtb_plan *plan, double *ms, int64_t *launches, int64_t *total_launches) {
+  if (!plan || !plan->has_run) return fail(GBXTB_ERR_ARG, "no singlepoint has run on this plan");
+  CK(cudaStreamSynchronize(plan->last_stream));
+  for (int c = 0; c < GBXTB_PROF_CLASSES; ++c) {
+    if (ms) ms[c] = plan->prof_ms[c];
+    if (launches) launches[c] = plan->prof_launches[c];
+  }
+  if (total_launches) *total_launches = plan->total_launches;
+  return GBXTB_OK;
+}
+
+int gbxtb_get_shell_potential(gbxtb_plan *plan, double *potential) {
+  if (!plan || !plan->has_run || !potential) return fail(GBXTB_ERR_ARG, "no singlepoint has run on this plan");
+  CK(cudaStreamSynchronize(plan->last_stream));
+  CK(cudaMemcpy(potential, plan->last_work.vout, sizeof(double) * plan->pl.nsh, cudaMemcpyDeviceToHost));
   return GBXTB_OK;
 }
 

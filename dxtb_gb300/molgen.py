@@ -54,11 +54,14 @@ def grow(natoms: int, seed: int) -> tuple[np.ndarray, np.ndarray]:
 
 
 def workload(config: int, count: int, nmin: int, nmax: int, perturb: float = 0.0,
-             log_uniform: bool = False) -> list[tuple[np.ndarray, np.ndarray]]:
+             log_uniform: bool = False, shard: int = 0) -> list[tuple[np.ndarray, np.ndarray]]:
     """``count`` molecules for workload ``config``: atom counts uniform (or
     log-uniform) in [nmin, nmax] drawn from seed ``1000*config + 999``;
-    positions optionally displaced by N(0, perturb) bohr."""
-    rng = np.random.Generator(np.random.PCG64(1000 * config + 999))
+    positions optionally displaced by N(0, perturb) bohr.  ``shard`` > 0
+    gives a further, disjoint set of the same distribution (seeds offset by
+    ``10**6 * shard``), used to give every GPU its own molecules."""
+    base = 10**6 * shard
+    rng = np.random.Generator(np.random.PCG64(base + 1000 * config + 999))
     if log_uniform:
         sizes = np.exp(rng.uniform(np.log(nmin), np.log(nmax + 1), size=count)).astype(int)
         sizes = np.clip(sizes, nmin, nmax)
@@ -66,9 +69,9 @@ def workload(config: int, count: int, nmin: int, nmax: int, perturb: float = 0.0
         sizes = rng.integers(nmin, nmax + 1, size=count)
     mols = []
     for i, n in enumerate(sizes):
-        num, pos = grow(int(n), 1000 * config + i)
+        num, pos = grow(int(n), base + 1000 * config + i)
         if perturb > 0.0:
-            prng = np.random.Generator(np.random.PCG64(1000 * config + i + 500_000))
+            prng = np.random.Generator(np.random.PCG64(base + 1000 * config + i + 500_000))
             pos = pos + prng.normal(scale=perturb, size=pos.shape)
         mols.append((num, pos))
     return mols
@@ -80,9 +83,9 @@ def c1_single() -> list:
     return [grow(20, 1000 * 0 + 0)]
 
 
-def c2_batch(count: int = 512) -> list:
+def c2_batch(count: int = 512, shard: int = 0) -> list:
     """Molecules of 10-120 atoms."""
-    return workload(1, count, 10, 120)
+    return workload(1, count, 10, 120, shard=shard)
 
 
 def c3_forces(count: int = 256) -> list:

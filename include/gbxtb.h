@@ -19,6 +19,12 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#if defined(__GNUC__)
+#define GBXTB_API __attribute__((visibility("default")))
+#else
+#define GBXTB_API
+#endif
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -84,19 +90,36 @@ typedef struct {
   double x_atol_max;      /* max norm of the potential change ("x_atol_max") */
   double kt;              /* electronic temperature in Hartree (fermi_etemp * k_B) */
   double broyden_alpha;   /* mixer step */
+  int32_t profile;        /* 1: time each kernel class with CUDA events (gbxtb_get_profile) */
+  int32_t reserved;
 } gbxtb_options;
 
+/* Kernel classes reported by gbxtb_get_profile. */
+#define GBXTB_PROF_ATOMS 0        /* coordination numbers, repulsion */
+#define GBXTB_PROF_SHELLPAIRS 1   /* overlap, H0, gamma */
+#define GBXTB_PROF_CHOLESKY 2     /* S = L L^T, L^-1 */
+#define GBXTB_PROF_FOCK 3         /* L^-1 F L^-T (two GEMMs) */
+#define GBXTB_PROF_TRIDIAG 4      /* Householder tridiagonalisation */
+#define GBXTB_PROF_BISECT 5       /* tridiagonal eigenvalues */
+#define GBXTB_PROF_FERMI 6        /* occupations */
+#define GBXTB_PROF_INVIT 7        /* tridiagonal eigenvectors */
+#define GBXTB_PROF_BACKTRANSFORM 8
+#define GBXTB_PROF_DENSITY 9      /* C = L^-T Y, P = C f C^T (two GEMMs) */
+#define GBXTB_PROF_MIX 10         /* charges, potential, mixing */
+#define GBXTB_PROF_FORCES 11      /* W, adjoint kernels */
+#define GBXTB_PROF_CLASSES 12
+
 /* Library version (GBXTB_VERSION). */
-int gbxtb_version(void);
+GBXTB_API int gbxtb_version(void);
 
 /* Message describing the last error on the calling thread. */
-const char *gbxtb_last_error(void);
+GBXTB_API const char *gbxtb_last_error(void);
 
 /* Upload the parameter tables to the current CUDA device.
  * Replaces dxtb's parameter loading (param/gfn1/load.py,
  * calculators/types/base.py:451-734 constructor). */
-int gbxtb_ctx_create(const gbxtb_params *params, gbxtb_ctx **out);
-void gbxtb_ctx_destroy(gbxtb_ctx *ctx);
+GBXTB_API int gbxtb_ctx_create(const gbxtb_params *params, gbxtb_ctx **out);
+GBXTB_API void gbxtb_ctx_destroy(gbxtb_ctx *ctx);
 
 /* Plan a batch of molecules: ragged atomic numbers (host), atom offsets
  * (host, nmol+1), total charge and number of unpaired electrons per molecule
@@ -105,21 +128,21 @@ void gbxtb_ctx_destroy(gbxtb_ctx *ctx);
  * basis/indexhelper.py:283-491 and scf/iterator.py:147-189).
  * *workspace_bytes receives the device scratch size needed by
  * gbxtb_singlepoint for this plan. */
-int gbxtb_plan_create(gbxtb_ctx *ctx, int32_t nmol, const int32_t *numbers,
+GBXTB_API int gbxtb_plan_create(gbxtb_ctx *ctx, int32_t nmol, const int32_t *numbers,
                       const int64_t *atom_offsets, const double *charge,
                       const int32_t *uhf, gbxtb_plan **out,
                       size_t *workspace_bytes);
-void gbxtb_plan_destroy(gbxtb_plan *plan);
+GBXTB_API void gbxtb_plan_destroy(gbxtb_plan *plan);
 
 /* Sizes of a plan: [nmol, natoms, nshells, naos, nmat_doubles, nshellpair_doubles]. */
-int gbxtb_plan_sizes(const gbxtb_plan *plan, int64_t *sizes6);
+GBXTB_API int gbxtb_plan_sizes(const gbxtb_plan *plan, int64_t *sizes6);
 
 /* Overlap and core Hamiltonian for ragged positions (bohr, [natoms][3]).
  * Outputs are per-molecule dense row-major nao x nao blocks, packed one after
  * another (offset of molecule m = sum_{k<m} nao_k^2).
  * Replaces integral/driver/pytorch/impls/overlap.py:147-243 and
  * xtb/base.py:251-360. */
-int gbxtb_integrals(gbxtb_plan *plan, const double *positions_dev,
+GBXTB_API int gbxtb_integrals(gbxtb_plan *plan, const double *positions_dev,
                     double *overlap_dev, double *hcore_dev, void *workspace_dev,
                     size_t workspace_bytes, void *stream);
 
@@ -127,7 +150,7 @@ int gbxtb_integrals(gbxtb_plan *plan, const double *positions_dev,
  * and the energy gradient dE/dR ([natoms][3], nullable; required when
  * opts->want_forces).  Replaces calculators/types/energy.py:78-402 (energy)
  * and calculators/types/autograd.py:82-201 (forces = -gradient). */
-int gbxtb_singlepoint(gbxtb_plan *plan, const gbxtb_options *opts,
+GBXTB_API int gbxtb_singlepoint(gbxtb_plan *plan, const gbxtb_options *opts,
                       const double *positions_dev, double *energy_dev,
                       double *charges_dev, double *gradient_dev,
                       void *workspace_dev, size_t workspace_bytes,
@@ -136,7 +159,24 @@ int gbxtb_singlepoint(gbxtb_plan *plan, const gbxtb_options *opts,
 /* Per-molecule status bits and SCF iteration counts of the last
  * gbxtb_singlepoint on this plan (host arrays of nmol). Synchronises the
  * stream of that call. */
-int gbxtb_get_status(gbxtb_plan *plan, int32_t *status, int32_t *iterations);
+GBXTB_API int gbxtb_get_status(gbxtb_plan *plan, int32_t *status, int32_t *iterations);
+
+/* Per-class device time (ms) and kernel-launch counts of the last
+ * gbxtb_singlepoint run with opts->profile = 1 (host arrays of
+ * GBXTB_PROF_CLASSES); *total_launches receives all kernel launches of that
+ * call (counted with or without profiling). */
+GBXTB_API int gbxtb_get_profile(gbxtb_plan *plan, double *ms, int64_t *launches, int64_t *total_launches);
+
+/* Shell-resolved SCF potential of the final state of the last
+ * gbxtb_singlepoint (host array of nshells, in plan order); the orbital
+ * potential of the reference (scf/base.py:701-727) is this value repeated
+ * over the 2l+1 orbitals of each shell.  Synchronises that call's stream. */
+GBXTB_API int gbxtb_get_shell_potential(gbxtb_plan *plan, double *potential);
+
+/* Measured FP64 FMA throughput of the current device in GFLOP/s (a short
+ * microbenchmark, ~10 ms); used as the roofline denominator of the
+ * FP64-bound kernels.  No counterpart in the reference. */
+GBXTB_API int gbxtb_fp64_peak(double *gflops);
 
 #ifdef __cplusplus
 }

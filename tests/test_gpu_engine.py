@@ -1,0 +1,193 @@
+"""GPU parity of the CUDA engine against the oracle and the reference's
+outputs.  Tolerances: energies 1e-8 Eh, forces 1e-6 Eh/bohr (the bar of the
+reference comparison), charges 1e-7 e; integrals 1e-12."""
+import warnings
+
+import numpy as np
+import pytest
+import torch
+
+from dxtb_gb300 import molgen
+from oracle import gfn1_oracle as go
+from tests.helpers import load_golden, same_state
+
+pytestmark = pytest.mark.gpu
+
+E_TOL = 1e-8
+F_TOL = 1e-6
+Q_TOL = 1e-7
+TIGHT = {"exclude": ["disp"], "maxiter": 300, "x_atol": 1e-10, "x_atol_max": 1e-10}
+
+
+def calc_for(numbers, **extra):
+    from dxtb_gb300 import GFN1Calculator
+
+    return GFN1Calculator(torch.as_tensor(np.asarray(numbers)), opts={**TIGHT, **extra})
+
+
+def pad(mols):
+    n = max(len(m[0]) for m in mols)
+    num = np.zeros((len(mols), n), dtype=np.int64)
+    pos = np.zeros((len(mols), n, 3))
+    for i, (a, b) in enumerate(mols):
+        num[i, :len(a)] = a
+        pos[i, :len(a)] = b
+    return num, pos
+
+
+@pytest.mark.parametrize("mol", load_golden("reference_mols.npz") + load_golden("synthetic.npz")[:6],
+                         ids=lambda m: m["name"])
+def test_integrals_match_oracle(mol):
+    num, pos = mol["numbers"], mol["positions"]
+    calc = calc_for(num)
+    (s, h), = calc.get_integrals(torch.tensor(pos, device="cuda"))
+    b = go.Basis(num)
+    s_ref = go.overlap(b, pos)
+    h_ref = go.core_hamiltonian(b, pos, s_ref, go.coordination_number(num, pos)).h0
+    assert np.abs(s.cpu().numpy() - s_ref).max() < 1e-12
+    assert np.abs(h.cpu().numpy() - h_ref).max() < 1e-12
+
+
+@pytest.mark.parametrize("mol", load_golden("reference_mols.npz"), ids=lambda m: m["name"])
+def test_reference_molecules(mol):
+    """Reference test geometries (incl. the open-shell NO2 and Si/Li
+    compounds with d shells) against the reference's energies, charges and
+    autograd forces."""
+    calc = calc_for(mol["numbers"])
+    pos = torch.tensor(mol["positions"], device="cuda")
+    res = calc.singlepoint(pos, chrg=mol["charge"], forces=True)
+    assert res.status[0] == 0
+    assert abs(res.energy.item() - mol["energy"]) < E_TOL
+    assert np.abs(res.charges.cpu().numpy() - mol["charges"]).max() < Q_TOL
+    assert np.abs(-res.gradient.cpu().numpy() - mol["forces"]).max() < F_TOL
+
+
+def test_synthetic_molecules_against_reference():
+    mols = load_golden("synthetic.npz")
+    num, pos = pad([(m["numbers"], m["positions"]) for m in mols])
+    calc = calc_for(num)
+    res = calc.singlepoint(torch.tensor(pos, device="cuda"), forces=True)
+    e = res.energy.cpu().numpy()
+    f = -res.gradient.cpu().numpy()
+    q = res.charges.cpu().numpy()
+    agree = 0
+    off = 0
+    for k, m in enumerate(mols):
+        n = len(m["numbers"])
+        assert res.status[k] == 0
+        if same_state(e[k], m["energy"]):
+            assert abs(e[k] - m["energy"]) < E_TOL, m["name"]
+            assert np.abs(q[off:off + n] - m["charges"]).max() < Q_TOL, m["name"]
+            assert np.abs(f[off:off + n] - m["forces"]).max() < F_TOL, m["name"]
+            agree += 1
+        off += n
+    assert agree >= len(mols) - 2
+
+
+def test_engine_replays_oracle_broyden():
+    """Same mixer on both sides: the GPU and the oracle follow the same SCF
+    trajectory (iteration counts) and agree to 1e-10 Eh."""
+    mols = molgen.c3_forces(4)
+    for num, pos in mols:
+        calc = calc_for(num)
+        res = calc.singlepoint(torch.tensor(pos, device="cuda"), forces=True)
+        r = go.singlepoint(num, pos, mixer="broyden")
+        assert abs(res.energy.item() - r.energy) < 1e-10
+        assert np.abs(-res.gradient.cpu().numpy() - r.forces).max() < 1e-8
+        assert abs(int(res.iterations[0]) - r.iterations) <= 2
+
+
+def test_batch_equals_single():
+    mols = molgen.c2_batch(6)
+    num, pos = pad(mols)
+    calc = calc_for(num)
+    rb = calc.singlepoint(torch.tensor(pos, device="cuda"), forces=True)
+    off = 0
+    for k, (n1, p1) in enumerate(mols):
+        rs = calc_for(n1).singlepoint(torch.tensor(p1, device="cuda"), forces=True)
+        n = len(n1)
+        assert rb.energy[k].item() == rs.energy.item()
+        assert torch.allclose(rb.gradient[off:off + n], rs.gradient, atol=1e-12, rtol=0)
+        off += n
+
+
+def test_autograd_matches_forces():
+    num, pos = molgen.c1_single()[0]
+    calc = calc_for(num)
+    p = torch.tensor(pos, device="cuda", requires_grad=True)
+    e = calc.get_energy(p)
+    (g,) = torch.autograd.grad(e, p)
+    f = calc.get_forces(torch.tensor(pos, device="cuda"))
+    assert torch.allclose(-g, f, atol=1e-12, rtol=0)
+    assert e.shape == ()
+
+
+def test_finite_differences():
+    """Central differences (h = 1e-4 bohr) on 8 random atoms of a perturbed
+    30-60-atom molecule, all displaced geometries in one batched call."""
+    num, pos = molgen.c3_forces(1)[0]
+    calc = calc_for(num)
+    f = calc.get_forces(torch.tensor(pos, device="cuda")).cpu().numpy()
+    rng = np.random.default_rng(7)
+    atoms = rng.choice(len(num), size=8, replace=False)
+    h = 1e-4
+    geoms = []
+    for a in atoms:
+        for x in range(3):
+            for sgn in (1.0, -1.0):
+                p = pos.copy()
+                p[a, x] += sgn * h
+                geoms.append(p)
+    nb = np.broadcast_to(num, (len(geoms), len(num))).copy()
+    calc_b = calc_for(nb)
+    e = calc_b.get_energy(torch.tensor(np.array(geoms), device="cuda")).cpu().numpy()
+    fd = -(e[0::2] - e[1::2]) / (2 * h)
+    an = np.array([f[a, x] for a in atoms for x in range(3)])
+    # the reference's energy carries ~1e-8 Eh noise from its Fermi tolerance
+    assert np.abs(fd - an).max() < 2e-4
+    assert np.median(np.abs(fd - an)) < 2e-5
+
+
+def test_maxiter_warning_and_error():
+    from dxtb_gb300 import SCFConvergenceError, SCFConvergenceWarning
+
+    num, pos = molgen.c1_single()[0]
+    calc = calc_for(num, maxiter=2)
+    with pytest.warns(SCFConvergenceWarning):
+        res = calc.singlepoint(torch.tensor(pos, device="cuda"))
+    assert res.status[0] & 1
+    calc = calc_for(num, maxiter=2, force_convergence=True)
+    with pytest.raises(SCFConvergenceError):
+        calc.singlepoint(torch.tensor(pos, device="cuda"))
+
+
+def test_input_errors():
+    from dxtb_gb300 import GFN1Calculator
+    from dxtb_gb300._lib import GbxtbError
+
+    with pytest.raises(ValueError):
+        GFN1Calculator(torch.tensor([1, 1]), opts={})  # D3 not excluded
+    with pytest.raises(ValueError):
+        GFN1Calculator(torch.tensor([1.0, 1.0]), opts=TIGHT)
+    calc = GFN1Calculator(torch.tensor([1, 1]), opts=TIGHT)
+    with pytest.raises(ValueError):
+        calc.get_energy(torch.zeros((2, 3), dtype=torch.float32, device="cuda"))
+    with pytest.raises(GbxtbError):
+        GFN1Calculator(torch.tensor([1, 87]), opts=TIGHT).get_energy(
+            torch.tensor([[0.0, 0, 0], [0, 0, 1.4]], dtype=torch.float64, device="cuda"))
+
+
+def test_charged_and_spin():
+    """Cation and explicit spin go through the same path as the reference
+    (electron count and alpha/beta split)."""
+    num, pos = molgen.c1_single()[0]
+    calc = calc_for(num)
+    p = torch.tensor(pos, device="cuda")
+    res = calc.singlepoint(p, chrg=1.0, spin=1)
+    r = go.singlepoint(num, pos, chrg=1.0, spin=1, mixer="broyden", forces=False)
+    assert abs(res.energy.item() - r.energy) < 1e-10
+    with warnings.catch_warnings():
+        warnings.simplefilter("error")
+        res2 = calc.singlepoint(p, chrg=2.0)
+    r2 = go.singlepoint(num, pos, chrg=2.0, mixer="broyden", forces=False)
+    assert abs(res2.energy.item() - r2.energy) < 1e-10
