@@ -23,8 +23,8 @@ namespace gbxtb {
 void launch_gemm(const DevPlan &pl, const Work &w, const int64_t *tile0, int64_t ntile, int mode,
                  int all, cudaStream_t s);
 void launch_tridiag(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s);
-void launch_bisect(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s);
-void launch_invit(const DevPlan &pl, const Work &w, cudaStream_t s);
+void launch_bisect(const DevPlan &pl, const Work &w, int maxn, double kt, cudaStream_t s);
+void launch_invit(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s);
 void launch_backtransform(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s);
 cudaError_t set_linalg_smem_limits(int maxn);
 void launch_count_active(const DevPlan &pl, const Work &w, cudaStream_t s);
@@ -105,9 +105,9 @@ struct Layout {
 Layout make_layout(const DevPlan &pl) {
   Layout L;
   const size_t d = sizeof(double), i4 = sizeof(int32_t);
-  for (int k = 0; k < 6; ++k) L.add(d * pl.nmat);          // S H0 Linv A Z P
+  for (int k = 0; k < 7; ++k) L.add(d * pl.nmat);          // S H0 Linv A Z P H0p
   L.add(d * 5 * pl.nmat);                                   // invit
-  for (int k = 0; k < 5; ++k) L.add(d * pl.nao);            // eig d e tau q
+  for (int k = 0; k < 6; ++k) L.add(d * pl.nao);            // eig d e tau q ldiag
   L.add(d * 2 * pl.nao);                                    // occ
   for (int k = 0; k < 7; ++k) L.add(d * pl.nsh);            // qsh vin vout vmix fprev xprev dedh
   L.add(d * kHistMax * pl.nsh);                             // hist_df
@@ -130,9 +130,9 @@ Work make_work(const DevPlan &pl, void *base) {
   auto D = [&]() { return reinterpret_cast<double *>(b + L.off[k++]); };
   auto I = [&]() { return reinterpret_cast<int32_t *>(b + L.off[k++]); };
   Work w{};
-  w.S = D(); w.H0 = D(); w.Linv = D(); w.A = D(); w.Z = D(); w.P = D();
+  w.S = D(); w.H0 = D(); w.Linv = D(); w.A = D(); w.Z = D(); w.P = D(); w.H0p = D();
   w.invit = D();
-  w.eig = D(); w.d = D(); w.e = D(); w.tau = D(); w.q = D();
+  w.eig = D(); w.d = D(); w.e = D(); w.tau = D(); w.q = D(); w.ldiag = D();
   w.occ = D();
   w.qsh = D(); w.vin = D(); w.vout = D(); w.vmix = D(); w.fprev = D(); w.xprev = D(); w.dedh = D();
   w.hist_df = D(); w.hist_u = D();
@@ -500,26 +500,28 @@ int gbxtb_singlepoint(gbxtb_plan *plan, const gbxtb_options *opts, const double 
   pf.end(GBXTB_PROF_SHELLPAIRS, 1);
   pf.begin(GBXTB_PROF_CHOLESKY);
   launch_cholesky(pl, w, s);
-  pf.end(GBXTB_PROF_CHOLESKY, 1);
+  // H0' = L^-1 H0 L^-T once per geometry (the potential is still zero)
+  launch_gemm(pl, w, plan->tile0, plan->ntile, 0, 0, s);
+  launch_gemm(pl, w, plan->tile0, plan->ntile, 5, 0, s);
+  pf.end(GBXTB_PROF_CHOLESKY, 3);
   CK(cudaGetLastError());
   // SCF: maxiter mixing iterations + the first evaluation + the final pass
   const int max_loops = opts->maxiter + 3;
   for (int it = 0; it < max_loops; ++it) {
     pf.begin(GBXTB_PROF_FOCK);
-    launch_gemm(pl, w, plan->tile0, plan->ntile, 0, 0, s);
-    launch_gemm(pl, w, plan->tile0, plan->ntile, 1, 0, s);
-    pf.end(GBXTB_PROF_FOCK, 2);
+    launch_gemm(pl, w, plan->tile0, plan->ntile, 6, 0, s);
+    pf.end(GBXTB_PROF_FOCK, 1);
     pf.begin(GBXTB_PROF_TRIDIAG);
     launch_tridiag(pl, w, plan->maxn, s);
     pf.end(GBXTB_PROF_TRIDIAG, 1);
     pf.begin(GBXTB_PROF_BISECT);
-    launch_bisect(pl, w, plan->maxn, s);
+    launch_bisect(pl, w, plan->maxn, opts->kt, s);
     pf.end(GBXTB_PROF_BISECT, 1);
     pf.begin(GBXTB_PROF_FERMI);
     launch_fermi(pl, w, opts->kt, opts->fermi_maxiter, s);
     pf.end(GBXTB_PROF_FERMI, 1);
     pf.begin(GBXTB_PROF_INVIT);
-    launch_invit(pl, w, s);
+    launch_invit(pl, w, plan->maxn, s);
     pf.end(GBXTB_PROF_INVIT, 1);
     pf.begin(GBXTB_PROF_BACKTRANSFORM);
     launch_backtransform(pl, w, plan->maxn, s);

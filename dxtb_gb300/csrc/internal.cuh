@@ -61,6 +61,8 @@ struct DevPlan {
 struct Work {
   // nao*nao blocks
   double *S, *H0, *Linv, *A, *Z, *P;
+  double *H0p;    // L^-1 H0 L^-T (orthogonal-basis core Hamiltonian), per geometry
+  double *ldiag;  // diagonal of the Cholesky factor L (per AO)
   double *invit;  // 5 * nmat: inverse-iteration LU factors
   // per AO
   double *eig, *d, *e, *tau, *occ, *q;  // occ: [2][nao_total]

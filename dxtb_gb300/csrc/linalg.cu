@@ -99,6 +99,14 @@ __global__ void __launch_bounds__(512) k_cholesky(DevPlan pl, Work w) {
       X[(int64_t)i * n + j] = -s / L[(int64_t)i * n + i];
     }
   }
+  __syncthreads();
+  // keep L itself: its transpose in the (unused) strict upper triangle of
+  // the L^-1 buffer, its diagonal in ldiag
+  for (int64_t t = threadIdx.x; t < (int64_t)n * n; t += blockDim.x) {
+    const int r = (int)(t / n), c = (int)(t % n);
+    if (c > r) X[t] = L[(int64_t)c * n + r];
+  }
+  for (int j = threadIdx.x; j < n; j += blockDim.x) w.ldiag[md.ao0 + j] = L[(int64_t)j * n + j];
 }
 
 // ---------------------------------------------------------------------------
@@ -108,6 +116,13 @@ __global__ void __launch_bounds__(512) k_cholesky(DevPlan pl, Work w) {
 //   mode 2: A = Linv^T * Y   (Y = Z, columns < kvec)
 //   mode 3: P = A diag(f) A^T  (f = occupation, K = kvec; symmetric)
 //   mode 4: Z = A diag(f e) A^T (energy-weighted density; symmetric)
+//   mode 5: H0p = Z * Linv^T (as mode 1, once per geometry)
+//   mode 6: A = H0p - (M + M^T)/2 with M = Linv diag(v) L (lower
+//           triangular): the Fock matrix in the orthogonal basis.  Because
+//           S = L L^T and S o (v_i + v_j) = diag(v) S + S diag(v),
+//           L^-1 (H0 - S o V / 2) L^-T = H0p - (L^-1 diag(v) L + transpose)/2,
+//           N^3/3 flops per SCF pass instead of 4 N^3/3.
+//   The strict upper triangle of the Linv buffer holds L^T, ldiag diag(L).
 // ---------------------------------------------------------------------------
 constexpr int BM = 64, BN = 64, BK = 16;
 
@@ -122,15 +137,19 @@ __global__ void __launch_bounds__(256) k_gemm(DevPlan pl, Work w, const int64_t 
   const int ti = local / nt, tj = local % nt;
   const int i0 = ti * BM, j0 = tj * BN;
   const int kvec = min(max(w.kvec[m], 0), n);
-  const bool sym = (mode == 1 || mode == 3 || mode == 4);
+  const bool sym = (mode == 1 || mode == 3 || mode == 4 || mode == 5 || mode == 6);
   const int ncol = (mode == 2) ? kvec : n;
   const int K = (mode == 3 || mode == 4) ? kvec : n;
   if (j0 >= ncol) return;
   if (sym && j0 > i0) return;
   int kmin = 0, kmax = K;
   if (mode == 0) kmax = min(K, i0 + BM);
-  if (mode == 1) kmax = min(K, j0 + BN);
+  if (mode == 1 || mode == 5) kmax = min(K, j0 + BN);
   if (mode == 2) kmin = (i0 / BK) * BK;
+  if (mode == 6) {
+    kmin = (j0 / BK) * BK;
+    kmax = min(K, i0 + BM);
+  }
 
   const double *Lv = w.Linv + md.mat0;
   const double *S = w.S + md.mat0, *H = w.H0 + md.mat0;
@@ -162,8 +181,9 @@ __global__ void __launch_bounds__(256) k_gemm(DevPlan pl, Work w, const int64_t 
       if (i < n && k < K) {
         switch (mode) {
           case 0: v = (k <= i) ? Lv[(int64_t)i * n + k] : 0.0; break;
-          case 1: v = Zs[(int64_t)i * n + k]; break;
+          case 1: case 5: v = Zs[(int64_t)i * n + k]; break;
           case 2: v = (k >= i) ? Lv[(int64_t)k * n + i] : 0.0; break;
+          case 6: v = (k <= i) ? Lv[(int64_t)i * n + k] * vin[aosh[k]] : 0.0; break;
           default: v = As[(int64_t)i * n + k]; break;
         }
       }
@@ -184,8 +204,11 @@ __global__ void __launch_bounds__(256) k_gemm(DevPlan pl, Work w, const int64_t 
             v = H[idx] - 0.5 * S[idx] * (vin[aosh[k]] + vin[aosh[j]]);
             break;
           }
-          case 1: v = (k <= j) ? Lv[(int64_t)j * n + k] : 0.0; break;
+          case 1: case 5: v = (k <= j) ? Lv[(int64_t)j * n + k] : 0.0; break;
           case 2: v = Zs[(int64_t)k * n + j]; break;
+          case 6:  // L(k, j): stored transposed above the diagonal
+            v = (k > j) ? Lv[(int64_t)j * n + k] : ((k == j) ? w.ldiag[md.ao0 + j] : 0.0);
+            break;
           case 3: v = As[(int64_t)j * n + k] * (occa[k] + occb[k]); break;
           default: v = As[(int64_t)j * n + k] * (occa[k] + occb[k]) * eig[k]; break;
         }
@@ -213,8 +236,11 @@ __global__ void __launch_bounds__(256) k_gemm(DevPlan pl, Work w, const int64_t 
     case 1: C = w.A + md.mat0; break;
     case 2: C = w.A + md.mat0; break;
     case 3: C = w.P + md.mat0; break;
+    case 5: C = w.H0p + md.mat0; break;
+    case 6: C = w.A + md.mat0; break;
     default: C = w.Z + md.mat0; break;
   }
+  const double *H0p = w.H0p + md.mat0;
 #pragma unroll
   for (int r = 0; r < 4; ++r) {
     const int i = i0 + ty * 4 + r;
@@ -225,8 +251,10 @@ __global__ void __launch_bounds__(256) k_gemm(DevPlan pl, Work w, const int64_t 
       if (j >= ncol) continue;
       if (sym) {
         if (j > i) continue;
-        C[(int64_t)i * n + j] = acc[r][c];
-        C[(int64_t)j * n + i] = acc[r][c];
+        double val = acc[r][c];
+        if (mode == 6) val = H0p[(int64_t)i * n + j] - ((i == j) ? val : 0.5 * val);
+        C[(int64_t)i * n + j] = val;
+        C[(int64_t)j * n + i] = val;
       } else {
         C[(int64_t)i * n + j] = acc[r][c];
       }
@@ -328,8 +356,50 @@ __global__ void __launch_bounds__(kTrdThreads) k_tridiag(DevPlan pl, Work w) {
 
 // ---------------------------------------------------------------------------
 // eigenvalues of the tridiagonal matrix by Sturm bisection
+//
+// The count of eigenvalues below x is the number of sign changes of the
+// leading principal minors p_j of T - x I (p_{j+1} = (d_j - x) p_j -
+// e_{j-1}^2 p_{j-1}); the recurrence needs no division (3 FP64 operations
+// per step instead of ~11 for the pivot form), is rescaled by exact powers
+// of two against overflow/underflow, and its signs are read as integer bits.
+// A zero minor is replaced by a tiny value of the opposite sign of its
+// predecessor (the pivot form's choice of a negative pivot).
+// All eigenvalues are bracketed to 1e-4 Eh first; only those that can carry
+// occupation (below the LUMO bracket + 60 kT + 0.01 Eh) are refined to full
+// precision: for the rest (E - E_F)/kT >= 50, where the occupation is
+// exactly zero and only their count enters the Fermi iteration.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_bisect(DevPlan pl, Work w) {
+__device__ __forceinline__ int sturm_count(const double *ds, const double *e2, int n, double x,
+                                           double pivmin) {
+  double pm = 1.0;           // p_{j-1}
+  double pc = ds[0] - x;     // p_j
+  if (pc == 0.0) pc = -pivmin;
+  int cnt = (int)((unsigned long long)__double_as_longlong(pc) >> 63);
+  for (int j = 1; j < n; ++j) {
+    double pn = fma(ds[j] - x, pc, -e2[j - 1] * pm);
+    const long long bits = __double_as_longlong(pn);
+    const long long bc = __double_as_longlong(pc);
+    if (pn == 0.0) pn = (bc < 0) ? pivmin : -pivmin;
+    const long long bn = __double_as_longlong(pn);
+    cnt += (int)((unsigned long long)(bn ^ bc) >> 63);
+    const int ex = (int)((bits >> 52) & 0x7ff);
+    pm = pc;
+    pc = pn;
+    if (ex > 1023 + 400) {         // |p| > 2^400: scale both down by 2^-400
+      pm *= 0x1p-400;
+      pc *= 0x1p-400;
+    } else if (ex < 1023 - 400) {  // |p| < 2^-400 (or zero): scale up
+      const int exm = (int)((__double_as_longlong(pm) >> 52) & 0x7ff);
+      if (exm < 1023 - 200) {
+        pm *= 0x1p+400;
+        pc *= 0x1p+400;
+      }
+    }
+  }
+  return cnt;
+}
+
+__global__ void __launch_bounds__(256) k_bisect(DevPlan pl, Work w, double kt) {
   const int m = blockIdx.x;
   if (w.phase[m] == kPhaseDone) return;
   const MolDesc md = pl.mol[m];
@@ -337,7 +407,9 @@ __global__ void __launch_bounds__(256) k_bisect(DevPlan pl, Work w) {
   extern __shared__ double sm[];
   double *ds = sm, *e2 = sm + n;
   __shared__ double red[32];
+  __shared__ double s_cut;
   const double *d = w.d + md.ao0, *e = w.e + md.ao0;
+  double *ev = w.eig + md.ao0;
   double glo = 1e300, ghi = -1e300, emax = 0.0;
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     ds[i] = d[i];
@@ -355,23 +427,38 @@ __global__ void __launch_bounds__(256) k_bisect(DevPlan pl, Work w) {
   glo -= 2.0 * kEps * tnorm * n + 1e-300;
   ghi += 2.0 * kEps * tnorm * n + 1e-300;
   const double pivmin = kSafeMin * fmax(1.0, emax);
+  // index of the lowest eigenvalue of the alpha channel that is empty at T=0
+  const int lumo = min(n - 1, (int)ceil(md.nel[0] - 5.0e-15));
+  // pass 1: every eigenvalue to 1e-4
+  // (every loop is bounded: a non-finite matrix ends with a garbage value,
+  //  which the SCF status check turns into an error, never in a hang)
   for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
     double lo = glo, hi = ghi;
-    for (int it = 0; it < 128; ++it) {
+    for (int it = 0; it < 96 && hi - lo > 1.0e-4; ++it) {
       const double mid = 0.5 * (lo + hi);
-      if (mid <= lo || mid >= hi) break;
-      int cnt = 0;
-      double q = ds[0] - mid;
-      if (fabs(q) < pivmin) q = -pivmin;
-      cnt += (q < 0.0);
-      for (int j = 1; j < n; ++j) {
-        q = (ds[j] - mid) - e2[j - 1] / q;
-        if (fabs(q) < pivmin) q = -pivmin;
-        cnt += (q < 0.0);
-      }
-      if (cnt <= idx) lo = mid; else hi = mid;
+      if (sturm_count(ds, e2, n, mid, pivmin) <= idx) lo = mid; else hi = mid;
     }
-    w.eig[md.ao0 + idx] = 0.5 * (lo + hi);
+    ev[idx] = lo;            // lower bracket
+    if (idx == lumo) s_cut = hi + 60.0 * kt + 0.01;
+  }
+  __syncthreads();
+  const double cut = s_cut;
+  // pass 2: full precision below the cut
+  for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
+    double lo = ev[idx];
+    double hi = lo + 1.0e-4;
+    if (lo < cut) {
+      hi = fmin(hi + 1.0e-4, ghi);
+      // re-establish a valid upper bracket
+      for (int it = 0; it < 64 && sturm_count(ds, e2, n, hi, pivmin) <= idx; ++it)
+        hi = fmin(hi + 1.0e-3, ghi + 1.0);
+      for (int it = 0; it < 128; ++it) {
+        const double mid = 0.5 * (lo + hi);
+        if (mid <= lo || mid >= hi) break;
+        if (sturm_count(ds, e2, n, mid, pivmin) <= idx) lo = mid; else hi = mid;
+      }
+    }
+    ev[idx] = 0.5 * (lo + hi);
   }
 }
 
@@ -386,15 +473,121 @@ __device__ __forceinline__ double start_value(int i, int j) {
   return ((double)(x & 0xffffff) / 16777216.0) - 0.5;
 }
 
-__global__ void __launch_bounds__(128) k_invit(DevPlan pl, Work w) {
+constexpr int kInvitThreads = 256;
+
+// One thread per eigenvector: LU factorisation with partial pivoting of
+// T - lambda I (factors kept in global scratch, interleaved over eigenvectors
+// so that the sequential sweeps of neighbouring threads are coalesced) and
+// one inverse-iteration solve.
+__device__ __forceinline__ void invit_factor(int n, int i, double lam, const double *d, const double *e,
+                                             double pert, double *U1, double *U2, double *U3, double *LM,
+                                             double *PV) {
+  double u1 = d[0] - lam;
+  double u2n = (n > 1) ? e[0] : 0.0;
+  for (int j = 0; j < n - 1; ++j) {
+    const double sub = e[j];
+    const double dn = d[j + 1] - lam;
+    const double sup2 = (j + 1 < n - 1) ? e[j + 1] : 0.0;
+    const int64_t o = (int64_t)j * n + i;
+    if (fabs(u1) >= fabs(sub)) {
+      const double mult = (u1 != 0.0) ? sub / u1 : 0.0;
+      U1[o] = (fabs(u1) < pert) ? ((u1 < 0.0) ? -pert : pert) : u1;
+      U2[o] = u2n;
+      U3[o] = 0.0;
+      LM[o] = mult;
+      PV[o] = 0.0;
+      u1 = dn - mult * u2n;
+      u2n = sup2;
+    } else {
+      const double mult = u1 / sub;
+      U1[o] = sub;
+      U2[o] = dn;
+      U3[o] = sup2;
+      LM[o] = mult;
+      PV[o] = 1.0;
+      u1 = u2n - mult * dn;
+      u2n = -mult * sup2;
+    }
+  }
+  const int64_t o = (int64_t)(n - 1) * n + i;
+  U1[o] = (fabs(u1) < pert) ? ((u1 < 0.0) ? -pert : pert) : u1;
+  U2[o] = 0.0;
+  U3[o] = 0.0;
+}
+
+__device__ __forceinline__ void invit_solve(int n, int i, const double *U1, const double *U2,
+                                            const double *U3, const double *LM, const double *PV,
+                                            double *Y) {
+  for (int j = 0; j < n - 1; ++j) {
+    const int64_t o = (int64_t)j * n + i;
+    const double yj = Y[o], yj1 = Y[o + n];
+    const double l = LM[o];
+    if (PV[o] != 0.0) {
+      Y[o] = yj1;
+      Y[o + n] = yj - l * yj1;
+    } else {
+      Y[o + n] = yj1 - l * yj;
+    }
+  }
+  double x1 = 0.0, x2 = 0.0, nrm = 0.0;
+  for (int j = n - 1; j >= 0; --j) {
+    const int64_t o = (int64_t)j * n + i;
+    const double s = (Y[o] - U2[o] * x1 - U3[o] * x2) / U1[o];
+    Y[o] = s;
+    x2 = x1;
+    x1 = s;
+    nrm = fmax(nrm, fabs(s));
+  }
+  const double inv = (nrm > 0.0) ? 1.0 / nrm : 1.0;
+  double s2 = 0.0;
+  for (int j = 0; j < n; ++j) {
+    const int64_t o = (int64_t)j * n + i;
+    const double y = Y[o] * inv;
+    Y[o] = y;
+    s2 += y * y;
+  }
+  const double in2 = 1.0 / sqrt(s2);
+  for (int j = 0; j < n; ++j) Y[(int64_t)j * n + i] *= in2;
+}
+
+// Modified Gram-Schmidt inside every cluster of close eigenvalues, one warp
+// per cluster, lanes over vector components.
+__device__ __forceinline__ void invit_cluster_mgs(int n, int kvec, const double *ev, double ctol,
+                                                  double *Y) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int c = wid; c < kvec; c += nw) {
+    if (c > 0 && ev[c] - ev[c - 1] <= ctol) continue;  // not a cluster start
+    int cend = c + 1;
+    while (cend < kvec && ev[cend] - ev[cend - 1] <= ctol) ++cend;
+    for (int i = c + 1; i < cend; ++i) {
+      for (int p = c; p < i; ++p) {
+        double dot = 0.0;
+        for (int j = lane; j < n; j += 32) dot += Y[(int64_t)j * n + p] * Y[(int64_t)j * n + i];
+        dot = warp_sum(dot);
+        for (int j = lane; j < n; j += 32) Y[(int64_t)j * n + i] -= dot * Y[(int64_t)j * n + p];
+      }
+      double s2 = 0.0;
+      for (int j = lane; j < n; j += 32) {
+        const double y = Y[(int64_t)j * n + i];
+        s2 += y * y;
+      }
+      s2 = warp_sum(s2);
+      const double in2 = 1.0 / sqrt(s2);
+      for (int j = lane; j < n; j += 32) Y[(int64_t)j * n + i] *= in2;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kInvitThreads) k_invit(DevPlan pl, Work w) {
   const int m = blockIdx.x;
   if (w.phase[m] == kPhaseDone) return;
   const MolDesc md = pl.mol[m];
   const int n = md.nao;
   const int kvec = min(max(w.kvec[m], 0), n);
-  const double *d = w.d + md.ao0, *e = w.e + md.ao0, *ev = w.eig + md.ao0;
+  extern __shared__ double sm[];
+  double *d = sm, *e = sm + n;
+  const double *ev = w.eig + md.ao0;
   double *Y = w.Z + md.mat0;
-  // scratch, interleaved by eigenvector index: X[j * n + i]
   double *U1 = w.invit + md.mat0 * 5;
   double *U2 = U1 + (int64_t)n * n;
   double *U3 = U2 + (int64_t)n * n;
@@ -403,96 +596,31 @@ __global__ void __launch_bounds__(128) k_invit(DevPlan pl, Work w) {
   __shared__ double red[32];
   double tl = 0.0;
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    d[i] = w.d[md.ao0 + i];
+    e[i] = (i < n - 1) ? w.e[md.ao0 + i] : 0.0;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
     const double el = (i > 0) ? fabs(e[i - 1]) : 0.0;
     const double er = (i < n - 1) ? fabs(e[i]) : 0.0;
     tl = fmax(tl, fabs(d[i]) + el + er);
   }
   const double tnorm = block_max(tl, red);
-  const double ctol = 1e-3 * tnorm;
+  // eigenvalues closer than 1e-4 |T| are orthogonalised explicitly; others
+  // come out orthogonal to eps |T| / gap <= 2e-12 from inverse iteration
+  const double ctol = 1e-4 * tnorm;
   const double pert = kEps * tnorm;
-  for (int c = threadIdx.x; c < kvec; c += blockDim.x) {
-    if (c > 0 && ev[c] - ev[c - 1] <= ctol) continue;  // not a cluster start
-    int cend = c + 1;
-    while (cend < kvec && ev[cend] - ev[cend - 1] <= ctol) ++cend;
-    for (int i = c; i < cend; ++i) {
-      const double lam = ev[i];
-      // LU with partial pivoting of T - lam I: rows j: u1 diag, u2 super, u3 super2
-      double u1 = d[0] - lam;
-      double u2n = (n > 1) ? e[0] : 0.0;  // current super diagonal of row j
-      for (int j = 0; j < n - 1; ++j) {
-        const double sub = e[j];
-        const double dn = d[j + 1] - lam;
-        const double sup2 = (j + 1 < n - 1) ? e[j + 1] : 0.0;
-        if (fabs(u1) >= fabs(sub)) {
-          const double mult = (u1 != 0.0) ? sub / u1 : 0.0;
-          U1[(int64_t)j * n + i] = u1;
-          U2[(int64_t)j * n + i] = u2n;
-          U3[(int64_t)j * n + i] = 0.0;
-          LM[(int64_t)j * n + i] = mult;
-          PV[(int64_t)j * n + i] = 0.0;
-          u1 = dn - mult * u2n;
-          u2n = sup2;
-        } else {
-          const double mult = u1 / sub;
-          U1[(int64_t)j * n + i] = sub;
-          U2[(int64_t)j * n + i] = dn;
-          U3[(int64_t)j * n + i] = sup2;
-          LM[(int64_t)j * n + i] = mult;
-          PV[(int64_t)j * n + i] = 1.0;
-          u1 = u2n - mult * dn;
-          u2n = -mult * sup2;
-        }
-      }
-      U1[(int64_t)(n - 1) * n + i] = u1;
-      U2[(int64_t)(n - 1) * n + i] = 0.0;
-      U3[(int64_t)(n - 1) * n + i] = 0.0;
-      for (int j = 0; j < n; ++j) {
-        double u = U1[(int64_t)j * n + i];
-        if (fabs(u) < pert) U1[(int64_t)j * n + i] = (u < 0.0) ? -pert : pert;
-      }
-      // start vector
-      for (int j = 0; j < n; ++j) Y[(int64_t)j * n + i] = start_value(i, j);
-      for (int itr = 0; itr < 3; ++itr) {
-        // apply L^-1 (row interchanges)
-        for (int j = 0; j < n - 1; ++j) {
-          const double yj = Y[(int64_t)j * n + i], yj1 = Y[(int64_t)(j + 1) * n + i];
-          const double l = LM[(int64_t)j * n + i];
-          if (PV[(int64_t)j * n + i] != 0.0) {
-            Y[(int64_t)j * n + i] = yj1;
-            Y[(int64_t)(j + 1) * n + i] = yj - l * yj1;
-          } else {
-            Y[(int64_t)(j + 1) * n + i] = yj1 - l * yj;
-          }
-        }
-        // back substitution with U
-        double x1 = 0.0, x2 = 0.0;  // x[j+1], x[j+2]
-        double nrm = 0.0;
-        for (int j = n - 1; j >= 0; --j) {
-          double s = Y[(int64_t)j * n + i] - U2[(int64_t)j * n + i] * x1 - U3[(int64_t)j * n + i] * x2;
-          s /= U1[(int64_t)j * n + i];
-          Y[(int64_t)j * n + i] = s;
-          x2 = x1;
-          x1 = s;
-          nrm = fmax(nrm, fabs(s));
-        }
-        // rescale, then orthogonalise against earlier members of the cluster
-        const double inv = (nrm > 0.0) ? 1.0 / nrm : 1.0;
-        for (int j = 0; j < n; ++j) Y[(int64_t)j * n + i] *= inv;
-        for (int p = c; p < i; ++p) {
-          double dot = 0.0;
-          for (int j = 0; j < n; ++j) dot += Y[(int64_t)j * n + p] * Y[(int64_t)j * n + i];
-          for (int j = 0; j < n; ++j) Y[(int64_t)j * n + i] -= dot * Y[(int64_t)j * n + p];
-        }
-        double s2 = 0.0;
-        for (int j = 0; j < n; ++j) {
-          const double y = Y[(int64_t)j * n + i];
-          s2 += y * y;
-        }
-        const double in2 = 1.0 / sqrt(s2);
-        for (int j = 0; j < n; ++j) Y[(int64_t)j * n + i] *= in2;
-      }
-    }
+  for (int i = threadIdx.x; i < kvec; i += blockDim.x) {
+    invit_factor(n, i, ev[i], d, e, pert, U1, U2, U3, LM, PV);
+    for (int j = 0; j < n; ++j) Y[(int64_t)j * n + i] = start_value(i, j);
+    invit_solve(n, i, U1, U2, U3, LM, PV, Y);
   }
+  __syncthreads();
+  invit_cluster_mgs(n, kvec, ev, ctol, Y);
+  __syncthreads();
+  for (int i = threadIdx.x; i < kvec; i += blockDim.x) invit_solve(n, i, U1, U2, U3, LM, PV, Y);
+  __syncthreads();
+  invit_cluster_mgs(n, kvec, ev, ctol, Y);
 }
 
 // ---------------------------------------------------------------------------
@@ -547,13 +675,13 @@ void launch_tridiag(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s) 
   k_tridiag<<<pl.nmol, kTrdThreads, smem, s>>>(pl, w);
 }
 
-void launch_bisect(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s) {
+void launch_bisect(const DevPlan &pl, const Work &w, int maxn, double kt, cudaStream_t s) {
   const size_t smem = sizeof(double) * 2 * (size_t)maxn;
-  k_bisect<<<pl.nmol, 256, smem, s>>>(pl, w);
+  k_bisect<<<pl.nmol, 256, smem, s>>>(pl, w, kt);
 }
 
-void launch_invit(const DevPlan &pl, const Work &w, cudaStream_t s) {
-  k_invit<<<pl.nmol, 128, 0, s>>>(pl, w);
+void launch_invit(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s) {
+  k_invit<<<pl.nmol, kInvitThreads, sizeof(double) * 2 * (size_t)maxn, s>>>(pl, w);
 }
 
 void launch_backtransform(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s) {
@@ -568,6 +696,8 @@ cudaError_t set_linalg_smem_limits(int maxn) {
     e = cudaFuncSetAttribute(k_tridiag, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(k_bisect, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_invit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
     if (e != cudaSuccess) return e;
   }
   return e;

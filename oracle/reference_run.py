@@ -72,10 +72,12 @@ def read_coord(path) -> tuple["np.ndarray", "np.ndarray"]:
     return np.array(nums, dtype=np.int64), np.array(pos, dtype=np.float64)
 
 
-def singlepoint(numbers, positions, chrg: float = 0.0, spin=None, forces: bool = True, opts=None) -> dict:
+def singlepoint(numbers, positions, chrg: float = 0.0, spin=None, forces: bool = True, opts=None,
+                analytical: bool = False) -> dict:
     """Energy (and autograd forces) of one molecule through the reference's
     ``GFN1Calculator`` (``calculators/types/energy.py:78-402``,
-    ``autograd.py:82-201``)."""
+    ``autograd.py:82-201``); with ``analytical`` also the reference's
+    analytical-gradient forces (``calculators/types/analytical.py:63-222``)."""
     _setup_path()
     import numpy as np
     import torch
@@ -107,4 +109,8 @@ def singlepoint(numbers, positions, chrg: float = 0.0, spin=None, forces: bool =
     if forces:
         (g,) = torch.autograd.grad(total, pos)
         out["forces"] = (-g).detach().numpy().copy()
+    if analytical:
+        calc2 = dxtb.calculators.GFN1Calculator(num, opts=o, dtype=torch.float64)
+        pos2 = torch.as_tensor(np.asarray(positions), dtype=torch.float64).clone().requires_grad_(True)
+        out["forces_analytical"] = calc2.forces_analytical(pos2, chrg=chrg, spin=spin).detach().numpy().copy()
     return out

@@ -5,7 +5,8 @@ container:
 * ``workload_batch_ref.npz``: all 512 molecules of the 10-120-atom batch
   workload: energy, atomic charges, SCF iterations, convergence flag;
 * ``workload_forces_ref.npz``: all 256 molecules of the perturbed 30-60-atom
-  force workload: energy, charges and autograd forces.
+  force workload: energy, charges, autograd forces (the reference's default
+  ``get_forces``) and its analytical-gradient forces (``forces_analytical``).
 
 Positions are not stored; they are regenerated from ``dxtb_gb300.molgen``
 (seeded) and checked against the stored atom counts and a coordinate
@@ -40,7 +41,7 @@ def _work(args):
     mols = molgen.c2_batch(512) if kind == "batch" else molgen.c3_forces(256)
     num, pos = mols[idx]
     t = time.time()
-    r = rr.singlepoint(num, pos, forces=forces)
+    r = rr.singlepoint(num, pos, forces=forces, analytical=forces)
     r["time"] = time.time() - t
     r["natom"] = len(num)
     r["checksum"] = float(np.sum(pos * np.arange(1, pos.size + 1).reshape(pos.shape)))
@@ -70,6 +71,7 @@ def run(kind: str, procs: int) -> None:
     out["converged"] = np.array([res[i]["converged"] for i in order])
     if forces:
         out["forces"] = np.concatenate([res[i]["forces"] for i in order])
+        out["forces_analytical"] = np.concatenate([res[i]["forces_analytical"] for i in order])
     path = HERE / f"workload_{kind}_ref.npz"
     np.savez_compressed(path, **out)
     print(f"wrote {path} ({path.stat().st_size} bytes) in {time.time() - t0:.0f}s")
