@@ -23,6 +23,8 @@ namespace gbxtb {
 void launch_gemm(const DevPlan &pl, const Work &w, const int64_t *tile0, int64_t ntile, int mode,
                  int all, cudaStream_t s);
 void launch_tridiag(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s);
+void launch_tridiag_cluster(const DevPlan &pl, const Work &w, const int32_t *mol_list, int count,
+                            int maxn, cudaStream_t s);
 void launch_bisect(const DevPlan &pl, const Work &w, int maxn, double kt, cudaStream_t s);
 void launch_invit(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s);
 void launch_backtransform(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s);
@@ -80,6 +82,7 @@ struct gbxtb_plan {
   Work last_work{};
   bool has_run = false;
   int32_t *h_active = nullptr;  // pinned
+  int num_sms = 0;
   // profiling
   cudaEvent_t ev[GBXTB_PROF_CLASSES][2] = {};
   bool ev_ready = false;
@@ -120,6 +123,7 @@ Layout make_layout(const DevPlan &pl) {
   L.add(d * 6 * pl.nmol);                                   // energy
   L.add(d * 2 * pl.nmol);                                   // resid
   L.add(i4 * 4);                                            // active
+  L.add(i4 * pl.nmol);                                      // active_list
   return L;
 }
 
@@ -142,6 +146,7 @@ Work make_work(const DevPlan &pl, void *base) {
   w.status = I(); w.phase = I(); w.iter = I(); w.kvec = I(); w.nhist = I();
   w.efermi = D(); w.energy = D(); w.resid = D();
   w.active = I();
+  w.active_list = I();
   return w;
 }
 
@@ -375,6 +380,11 @@ int gbxtb_plan_create(gbxtb_ctx *ctx, int32_t nmol, const int32_t *numbers,
     delete pl;
     return cuda_fail(e, "cudaMallocHost");
   }
+  {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&pl->num_sms, cudaDevAttrMultiProcessorCount, dev);
+  }
   pl->ws_bytes = make_layout(d).total;
   *workspace_bytes = pl->ws_bytes;
   *out = pl;
@@ -507,12 +517,17 @@ int gbxtb_singlepoint(gbxtb_plan *plan, const gbxtb_options *opts, const double 
   CK(cudaGetLastError());
   // SCF: maxiter mixing iterations + the first evaluation + the final pass
   const int max_loops = opts->maxiter + 3;
+  int active = pl.nmol;  // molecules iterating (known after each pass)
   for (int it = 0; it < max_loops; ++it) {
     pf.begin(GBXTB_PROF_FOCK);
     launch_gemm(pl, w, plan->tile0, plan->ntile, 6, 0, s);
     pf.end(GBXTB_PROF_FOCK, 1);
     pf.begin(GBXTB_PROF_TRIDIAG);
-    launch_tridiag(pl, w, plan->maxn, s);
+    // fewer molecules than SMs: spread each molecule over a cluster of SMs
+    if (it > 0 && active <= plan->num_sms)
+      launch_tridiag_cluster(pl, w, w.active_list, active, plan->maxn, s);
+    else
+      launch_tridiag(pl, w, plan->maxn, s);
     pf.end(GBXTB_PROF_TRIDIAG, 1);
     pf.begin(GBXTB_PROF_BISECT);
     launch_bisect(pl, w, plan->maxn, opts->kt, s);
@@ -538,7 +553,8 @@ int gbxtb_singlepoint(gbxtb_plan *plan, const gbxtb_options *opts, const double 
     CK(cudaMemcpyAsync(plan->h_active, w.active, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     pf.harvest();
-    if (plan->h_active[0] == 0) break;
+    active = plan->h_active[0];
+    if (active == 0) break;
   }
   launch_energies(p, pl, w, opts->kt, energy_dev, charges_dev, s);
   plan->total_launches += 1;

@@ -79,6 +79,7 @@ struct Work {
   double *energy;   // [nmol][6]: total, rep, h0, es2, es3, fermi
   double *resid;    // [nmol][2]: L2, max norm of the last potential change
   int32_t *active;  // [1]: molecules not yet done
+  int32_t *active_list;  // [nmol]: indices of those molecules
 };
 
 // ---------------------------------------------------------------------------

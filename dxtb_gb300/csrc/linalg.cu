@@ -25,6 +25,9 @@
 #include "internal.cuh"
 
 #include <cmath>
+#include <cooperative_groups.h>
+
+namespace cg = cooperative_groups;
 
 namespace gbxtb {
 
@@ -309,17 +312,18 @@ __global__ void __launch_bounds__(kTrdThreads) k_tridiag(DevPlan pl, Work w) {
     __syncthreads();
     const double tk = sc[0], scale = sc[1];
     if (tk == 0.0) {
-      // no reflection needed: store a zero reflector
-      for (int t = threadIdx.x; t < m1; t += blockDim.x) A[(int64_t)(k + 1 + t) * n + k] = (t == 0) ? 1.0 : 0.0;
+      // no reflection needed (tau = 0 makes the stored vector irrelevant)
       __syncthreads();
       continue;
     }
     for (int t = threadIdx.x; t < m1; t += blockDim.x) {
       double v = (t == 0) ? 1.0 : A[(int64_t)(k + 1 + t) * n + k] * scale;
       vs[t] = v;
-      A[(int64_t)(k + 1 + t) * n + k] = v;
     }
     __syncthreads();
+    // the reflector is kept in row k (contiguous), which the trailing
+    // update never touches again
+    for (int t = threadIdx.x; t < m1; t += blockDim.x) A[(int64_t)k * n + k + 1 + t] = vs[t];
     // p = tau * A22 v   (warp per row)
     for (int i = wid; i < m1; i += nw) {
       const double *row = A + (int64_t)(k + 1 + i) * n + (k + 1);
@@ -352,6 +356,126 @@ __global__ void __launch_bounds__(kTrdThreads) k_tridiag(DevPlan pl, Work w) {
       d[0] = A[0];
     }
   }
+}
+
+// ---------------------------------------------------------------------------
+// Householder tridiagonalisation on a thread-block cluster (8 SMs per
+// molecule) for latency: when few molecules are still iterating, one SM per
+// molecule leaves the GPU idle.  Rows are owned cyclically (row i by CTA
+// i mod 8); every CTA rebuilds the reflector from the column in L2, forms
+// p = tau A v and the rank-2 update for its own rows, and the two global
+// quantities of a step (p.v and the vector w) are exchanged through
+// distributed shared memory between three cluster barriers.  Matrix reads
+// bypass L1 (ld.global.cg) since other SMs of the cluster write the rows.
+// Same arithmetic and storage conventions as k_tridiag.
+// ---------------------------------------------------------------------------
+constexpr int kClusterSize = 8;
+constexpr int kTrdClThreads = 256;
+
+__global__ void __cluster_dims__(kClusterSize, 1, 1) __launch_bounds__(kTrdClThreads)
+    k_tridiag_cluster(DevPlan pl, Work w, const int32_t *mol_list) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const int m = mol_list[blockIdx.x / kClusterSize];
+  const MolDesc md = pl.mol[m];
+  const int n = md.nao;
+  double *A = w.A + md.mat0;
+  double *d = w.d + md.ao0, *e = w.e + md.ao0, *tau = w.tau + md.ao0;
+  extern __shared__ double sm[];
+  double *vs = sm;          // [n] full reflector
+  double *ws = sm + n;      // [n] p, then w, for own rows; full w after gather
+  __shared__ double red[32];
+  __shared__ double kpart;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const bool done = (w.phase[m] == kPhaseDone);  // uniform over the cluster
+  if (!done) {
+    for (int k = 0; k + 2 < n; ++k) {
+      const int m1 = n - k - 1;
+      // column x = A[k+1.., k] (rebuilt redundantly by every CTA)
+      double part = 0.0;
+      for (int t = 1 + threadIdx.x; t < m1; t += blockDim.x) {
+        const double x = __ldcg(A + (int64_t)(k + 1 + t) * n + k);
+        part += x * x;
+      }
+      const double xn2 = block_sum(part, red);
+      const double alpha = __ldcg(A + (int64_t)(k + 1) * n + k);
+      double tk = 0.0, scale = 0.0, beta = alpha;
+      if (xn2 != 0.0) {
+        beta = -copysign(sqrt(alpha * alpha + xn2), alpha);
+        tk = (beta - alpha) / beta;
+        scale = 1.0 / (alpha - beta);
+      }
+      if (rank == 0 && threadIdx.x == 0) {
+        d[k] = __ldcg(A + (int64_t)k * n + k);
+        e[k] = beta;
+        tau[k] = tk;
+      }
+      if (tk == 0.0) {
+        cluster.sync();
+        continue;
+      }
+      for (int t = threadIdx.x; t < m1; t += blockDim.x)
+        vs[t] = (t == 0) ? 1.0 : __ldcg(A + (int64_t)(k + 1 + t) * n + k) * scale;
+      __syncthreads();
+      if (rank == 0)
+        for (int t = threadIdx.x; t < m1; t += blockDim.x) A[(int64_t)k * n + k + 1 + t] = vs[t];
+      // p = tau A22 v for own rows (warp per row)
+      double pv = 0.0;
+      for (int t0 = wid; ; t0 += nw) {
+        // own rows: global row i = k+1+t with i % C == rank
+        const int first = (rank - (k + 1) % kClusterSize + kClusterSize) % kClusterSize;
+        const int t = first + t0 * kClusterSize;
+        if (t >= m1) break;
+        const double *row = A + (int64_t)(k + 1 + t) * n + (k + 1);
+        double sacc = 0.0;
+        for (int j = lane; j < m1; j += 32) sacc += __ldcg(row + j) * vs[j];
+        sacc = warp_sum(sacc) * tk;
+        if (lane == 0) {
+          ws[t] = sacc;
+          pv += sacc * vs[t];
+        }
+      }
+      const double kp = block_sum(pv, red);
+      if (threadIdx.x == 0) kpart = kp;
+      cluster.sync();
+      double K = 0.0;
+      for (int r = 0; r < kClusterSize; ++r) K += *cluster.map_shared_rank(&kpart, r);
+      const double half = 0.5 * tk * K;
+      {
+        const int first = (rank - (k + 1) % kClusterSize + kClusterSize) % kClusterSize;
+        for (int t = first + threadIdx.x * kClusterSize; t < m1; t += blockDim.x * kClusterSize)
+          ws[t] -= half * vs[t];
+      }
+      cluster.sync();
+      // gather w of all rows into local shared memory
+      double *wl = sm + 2 * n;  // [n]
+      for (int t = threadIdx.x; t < m1; t += blockDim.x) {
+        const int owner = (k + 1 + t) % kClusterSize;
+        wl[t] = *cluster.map_shared_rank(ws + t, owner);
+      }
+      __syncthreads();
+      // A22 -= v w^T + w v^T on own rows
+      {
+        const int first = (rank - (k + 1) % kClusterSize + kClusterSize) % kClusterSize;
+        for (int t = first + wid * kClusterSize; t < m1; t += nw * kClusterSize) {
+          double *row = A + (int64_t)(k + 1 + t) * n + (k + 1);
+          const double vi = vs[t], wi = wl[t];
+          for (int j = lane; j < m1; j += 32) row[j] -= vi * wl[j] + wi * vs[j];
+        }
+      }
+      cluster.sync();
+    }
+    if (rank == 0 && threadIdx.x == 0) {
+      if (n >= 2) {
+        d[n - 2] = __ldcg(A + (int64_t)(n - 2) * n + (n - 2));
+        d[n - 1] = __ldcg(A + (int64_t)(n - 1) * n + (n - 1));
+        e[n - 2] = __ldcg(A + (int64_t)(n - 1) * n + (n - 2));
+      } else {
+        d[0] = __ldcg(A);
+      }
+    }
+  }
+  cluster.sync();
 }
 
 // ---------------------------------------------------------------------------
@@ -399,8 +523,11 @@ __device__ __forceinline__ int sturm_count(const double *ds, const double *e2, i
   return cnt;
 }
 
+constexpr int kBisectSplit = 4;
+
 __global__ void __launch_bounds__(256) k_bisect(DevPlan pl, Work w, double kt) {
   const int m = blockIdx.x;
+  const int part = blockIdx.y;  // eigenvalue indices part, part + split, ...
   if (w.phase[m] == kPhaseDone) return;
   const MolDesc md = pl.mol[m];
   const int n = md.nao;
@@ -429,22 +556,31 @@ __global__ void __launch_bounds__(256) k_bisect(DevPlan pl, Work w, double kt) {
   const double pivmin = kSafeMin * fmax(1.0, emax);
   // index of the lowest eigenvalue of the alpha channel that is empty at T=0
   const int lumo = min(n - 1, (int)ceil(md.nel[0] - 5.0e-15));
-  // pass 1: every eigenvalue to 1e-4
+  // pass 1: every eigenvalue of this part to 1e-4, plus (thread 0) the LUMO
+  // bracket that fixes the refinement window
   // (every loop is bounded: a non-finite matrix ends with a garbage value,
   //  which the SCF status check turns into an error, never in a hang)
-  for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
+  const int stride = blockDim.x * kBisectSplit;
+  if (threadIdx.x == 0) {
+    double lo = glo, hi = ghi;
+    for (int it = 0; it < 96 && hi - lo > 1.0e-4; ++it) {
+      const double mid = 0.5 * (lo + hi);
+      if (sturm_count(ds, e2, n, mid, pivmin) <= lumo) lo = mid; else hi = mid;
+    }
+    s_cut = hi + 60.0 * kt + 0.01;
+  }
+  for (int idx = part * blockDim.x + threadIdx.x; idx < n; idx += stride) {
     double lo = glo, hi = ghi;
     for (int it = 0; it < 96 && hi - lo > 1.0e-4; ++it) {
       const double mid = 0.5 * (lo + hi);
       if (sturm_count(ds, e2, n, mid, pivmin) <= idx) lo = mid; else hi = mid;
     }
     ev[idx] = lo;            // lower bracket
-    if (idx == lumo) s_cut = hi + 60.0 * kt + 0.01;
   }
   __syncthreads();
   const double cut = s_cut;
   // pass 2: full precision below the cut
-  for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
+  for (int idx = part * blockDim.x + threadIdx.x; idx < n; idx += stride) {
     double lo = ev[idx];
     double hi = lo + 1.0e-4;
     if (lo < cut) {
@@ -624,11 +760,15 @@ __global__ void __launch_bounds__(kInvitThreads) k_invit(DevPlan pl, Work w) {
 }
 
 // ---------------------------------------------------------------------------
-// back-transformation Y <- Q Y, Q = H_0 ... H_{n-3}; thread per column
+// back-transformation Y <- Q Y, Q = H_0 ... H_{n-3}
+// A block owns 32 eigenvector columns and splits the rows over 8 warps:
+// per reflector, partial dot products per warp, one reduction in shared
+// memory, then every warp updates its rows (coalesced 256-byte rows of Y).
 // ---------------------------------------------------------------------------
-constexpr int kBtCols = 128;
+constexpr int kBtCols = 32;
+constexpr int kBtGroups = 8;
 
-__global__ void __launch_bounds__(kBtCols) k_backtransform(DevPlan pl, Work w) {
+__global__ void __launch_bounds__(kBtCols * kBtGroups) k_backtransform(DevPlan pl, Work w) {
   const int m = blockIdx.y;
   if (w.phase[m] == kPhaseDone) return;
   const MolDesc md = pl.mol[m];
@@ -640,17 +780,32 @@ __global__ void __launch_bounds__(kBtCols) k_backtransform(DevPlan pl, Work w) {
   const double *tau = w.tau + md.ao0;
   double *Y = w.Z + md.mat0;
   extern __shared__ double vsm[];
-  const int c = c0 + threadIdx.x;
+  __shared__ double part[kBtGroups][kBtCols];
+  __shared__ double sfac[kBtCols];
+  const int col = threadIdx.x & (kBtCols - 1), rg = threadIdx.x / kBtCols;
+  const int c = c0 + col;
+  const bool active = c < kvec;
   for (int k = n - 3; k >= 0; --k) {
-    const int m1 = n - k - 1;
-    for (int t = threadIdx.x; t < m1; t += blockDim.x) vsm[t] = A[(int64_t)(k + 1 + t) * n + k];
-    __syncthreads();
     const double tk = tau[k];
-    if (tk != 0.0 && c < kvec) {
-      double s = 0.0;
-      for (int r = 0; r < m1; ++r) s += vsm[r] * Y[(int64_t)(k + 1 + r) * n + c];
-      s *= tk;
-      for (int r = 0; r < m1; ++r) Y[(int64_t)(k + 1 + r) * n + c] -= s * vsm[r];
+    if (tk == 0.0) continue;  // uniform across the block
+    const int m1 = n - k - 1;
+    for (int t = threadIdx.x; t < m1; t += blockDim.x) vsm[t] = A[(int64_t)k * n + k + 1 + t];
+    __syncthreads();
+    double s = 0.0;
+    if (active)
+      for (int r = rg; r < m1; r += kBtGroups) s += vsm[r] * Y[(int64_t)(k + 1 + r) * n + c];
+    part[rg][col] = s;
+    __syncthreads();
+    if (rg == 0) {
+      double t = 0.0;
+#pragma unroll
+      for (int g = 0; g < kBtGroups; ++g) t += part[g][col];
+      sfac[col] = t * tk;
+    }
+    __syncthreads();
+    if (active) {
+      const double f = sfac[col];
+      for (int r = rg; r < m1; r += kBtGroups) Y[(int64_t)(k + 1 + r) * n + c] -= f * vsm[r];
     }
     __syncthreads();
   }
@@ -675,9 +830,18 @@ void launch_tridiag(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s) 
   k_tridiag<<<pl.nmol, kTrdThreads, smem, s>>>(pl, w);
 }
 
+// Cluster tridiagonalisation for the molecules listed in mol_list (device).
+void launch_tridiag_cluster(const DevPlan &pl, const Work &w, const int32_t *mol_list, int count,
+                            int maxn, cudaStream_t s) {
+  if (count <= 0) return;
+  const size_t smem = sizeof(double) * 3 * (size_t)maxn;
+  k_tridiag_cluster<<<count * kClusterSize, kTrdClThreads, smem, s>>>(pl, w, mol_list);
+}
+
 void launch_bisect(const DevPlan &pl, const Work &w, int maxn, double kt, cudaStream_t s) {
   const size_t smem = sizeof(double) * 2 * (size_t)maxn;
-  k_bisect<<<pl.nmol, 256, smem, s>>>(pl, w, kt);
+  dim3 grid(pl.nmol, kBisectSplit);
+  k_bisect<<<grid, 256, smem, s>>>(pl, w, kt);
 }
 
 void launch_invit(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s) {
@@ -686,7 +850,7 @@ void launch_invit(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s) {
 
 void launch_backtransform(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s) {
   dim3 grid((maxn + kBtCols - 1) / kBtCols, pl.nmol);
-  k_backtransform<<<grid, kBtCols, sizeof(double) * (size_t)maxn, s>>>(pl, w);
+  k_backtransform<<<grid, kBtCols * kBtGroups, sizeof(double) * (size_t)maxn, s>>>(pl, w);
 }
 
 cudaError_t set_linalg_smem_limits(int maxn) {
@@ -698,6 +862,11 @@ cudaError_t set_linalg_smem_limits(int maxn) {
     e = cudaFuncSetAttribute(k_bisect, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(k_invit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
+    if (e != cudaSuccess) return e;
+  }
+  const size_t need3 = sizeof(double) * 3 * (size_t)maxn;
+  if (need3 > 48 * 1024) {
+    e = cudaFuncSetAttribute(k_tridiag_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need3);
     if (e != cudaSuccess) return e;
   }
   return e;

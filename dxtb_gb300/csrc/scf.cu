@@ -337,12 +337,32 @@ __global__ void __launch_bounds__(kMixThreads) k_charges_mix(DevParams p, DevPla
   if (threadIdx.x == 0) w.nhist[m] = nst + 1;
 }
 
+// Count and list the molecules that still iterate (in index order).
 __global__ void k_count_active(DevPlan pl, Work w) {
-  __shared__ double red[32];
-  double c = 0.0;
-  for (int m = threadIdx.x; m < pl.nmol; m += blockDim.x) c += (w.phase[m] != kPhaseDone) ? 1.0 : 0.0;
-  c = block_sum(c, red);
-  if (threadIdx.x == 0) w.active[0] = (int)c;
+  __shared__ int s_base;
+  if (threadIdx.x == 0) s_base = 0;
+  __syncthreads();
+  for (int m0 = 0; m0 < pl.nmol; m0 += blockDim.x) {
+    const int m = m0 + threadIdx.x;
+    const int act = (m < pl.nmol && w.phase[m] != kPhaseDone) ? 1 : 0;
+    // block-wide exclusive scan of act
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int incl = act;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    __shared__ int wsum[32];
+    if (lane == 31) wsum[wid] = incl;
+    __syncthreads();
+    int off = 0;
+    for (int k = 0; k < wid; ++k) off += wsum[k];
+    if (act) w.active_list[s_base + off + incl - 1] = m;
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) s_base += off + incl;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) w.active[0] = s_base;
 }
 
 __global__ void k_outputs(DevPlan pl, Work w, double *energy_out, double *charges_out) {
