@@ -55,7 +55,7 @@ class Options(C.Structure):
         ("kt", C.c_double),
         ("broyden_alpha", C.c_double),
         ("profile", C.c_int32),
-        ("reserved", C.c_int32),
+        ("mixed_precision", C.c_int32),
     ]
 
 

@@ -56,6 +56,7 @@ DEFAULT_OPTS = {
     "broyden_memory": 20,
     "verbosity": 0,
     "profile": False,        # per-stage device timings (last_profile)
+    "mixed_precision": True,  # FP32 linear algebra in the early SCF passes
 }
 _ACCEPTED_IGNORED = {"scf_mode", "scp_mode", "int_driver", "int_level", "batch_mode", "damp",
                      "damp_init", "mix_guess", "cache_enabled", "timer", "strict", "log_level"}
@@ -264,6 +265,7 @@ class GFN1Calculator:
         opt.kt = float(o["fermi_etemp"]) * params.KELVIN2AU
         opt.broyden_alpha = float(o["broyden_alpha"])
         opt.profile = 1 if o["profile"] else 0
+        opt.mixed_precision = 1 if o["mixed_precision"] else 0
         return opt
 
     def _run(self, positions: torch.Tensor, chrg=0, spin=None, forces: bool = False) -> Result:

@@ -23,6 +23,7 @@ namespace gbxtb {
 void launch_gemm(const DevPlan &pl, const Work &w, const int64_t *tile0, int64_t ntile, int mode,
                  int all, cudaStream_t s);
 void launch_tridiag(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s);
+void launch_lowp_copies(const DevPlan &pl, const Work &w, cudaStream_t s);
 void launch_tridiag_cluster(const DevPlan &pl, const Work &w, const int32_t *mol_list, int count,
                             int maxn, cudaStream_t s);
 void launch_bisect(const DevPlan &pl, const Work &w, int maxn, double kt, cudaStream_t s);
@@ -108,7 +109,7 @@ struct Layout {
 Layout make_layout(const DevPlan &pl) {
   Layout L;
   const size_t d = sizeof(double), i4 = sizeof(int32_t);
-  for (int k = 0; k < 7; ++k) L.add(d * pl.nmat);          // S H0 Linv A Z P H0p
+  for (int k = 0; k < 8; ++k) L.add(d * pl.nmat);          // S H0 Linv A Z P H0p lo
   L.add(d * 5 * pl.nmat);                                   // invit
   for (int k = 0; k < 6; ++k) L.add(d * pl.nao);            // eig d e tau q ldiag
   L.add(d * 2 * pl.nao);                                    // occ
@@ -118,7 +119,7 @@ Layout make_layout(const DevPlan &pl) {
   L.add(d * pl.ngam);                                       // gam
   for (int k = 0; k < 4; ++k) L.add(d * pl.natom);          // cn erep qat dedcn
   L.add(d * 3 * pl.natom);                                  // grad
-  for (int k = 0; k < 5; ++k) L.add(i4 * pl.nmol);          // status phase iter kvec nhist
+  for (int k = 0; k < 6; ++k) L.add(i4 * pl.nmol);          // status phase iter kvec nhist prec
   L.add(d * 2 * pl.nmol);                                   // efermi
   L.add(d * 6 * pl.nmol);                                   // energy
   L.add(d * 2 * pl.nmol);                                   // resid
@@ -134,7 +135,7 @@ Work make_work(const DevPlan &pl, void *base) {
   auto D = [&]() { return reinterpret_cast<double *>(b + L.off[k++]); };
   auto I = [&]() { return reinterpret_cast<int32_t *>(b + L.off[k++]); };
   Work w{};
-  w.S = D(); w.H0 = D(); w.Linv = D(); w.A = D(); w.Z = D(); w.P = D(); w.H0p = D();
+  w.S = D(); w.H0 = D(); w.Linv = D(); w.A = D(); w.Z = D(); w.P = D(); w.H0p = D(); w.lo = D();
   w.invit = D();
   w.eig = D(); w.d = D(); w.e = D(); w.tau = D(); w.q = D(); w.ldiag = D();
   w.occ = D();
@@ -143,7 +144,7 @@ Work make_work(const DevPlan &pl, void *base) {
   w.gam = D();
   w.cn = D(); w.erep = D(); w.qat = D(); w.dedcn = D();
   w.grad = D();
-  w.status = I(); w.phase = I(); w.iter = I(); w.kvec = I(); w.nhist = I();
+  w.status = I(); w.phase = I(); w.iter = I(); w.kvec = I(); w.nhist = I(); w.prec = I();
   w.efermi = D(); w.energy = D(); w.resid = D();
   w.active = I();
   w.active_list = I();
@@ -499,6 +500,8 @@ int gbxtb_singlepoint(gbxtb_plan *plan, const gbxtb_options *opts, const double 
   CK(cudaMemsetAsync(w.iter, 0, sizeof(int32_t) * pl.nmol, s));
   CK(cudaMemsetAsync(w.kvec, 0, sizeof(int32_t) * pl.nmol, s));
   CK(cudaMemsetAsync(w.nhist, 0, sizeof(int32_t) * pl.nmol, s));
+  // 0: the first passes run in FP32; any non-zero byte pattern means FP64
+  CK(cudaMemsetAsync(w.prec, opts->mixed_precision ? 0 : 1, sizeof(int32_t) * pl.nmol, s));
   CK(cudaMemsetAsync(w.vin, 0, sizeof(double) * pl.nsh, s));
   CK(cudaMemsetAsync(w.energy, 0, sizeof(double) * 6 * pl.nmol, s));
   // geometry-dependent terms
@@ -513,7 +516,8 @@ int gbxtb_singlepoint(gbxtb_plan *plan, const gbxtb_options *opts, const double 
   // H0' = L^-1 H0 L^-T once per geometry (the potential is still zero)
   launch_gemm(pl, w, plan->tile0, plan->ntile, 0, 0, s);
   launch_gemm(pl, w, plan->tile0, plan->ntile, 5, 0, s);
-  pf.end(GBXTB_PROF_CHOLESKY, 3);
+  if (opts->mixed_precision) launch_lowp_copies(pl, w, s);
+  pf.end(GBXTB_PROF_CHOLESKY, opts->mixed_precision ? 4 : 3);
   CK(cudaGetLastError());
   // SCF: maxiter mixing iterations + the first evaluation + the final pass
   const int max_loops = opts->maxiter + 3;

@@ -62,6 +62,8 @@ struct Work {
   // nao*nao blocks
   double *S, *H0, *Linv, *A, *Z, *P;
   double *H0p;    // L^-1 H0 L^-T (orthogonal-basis core Hamiltonian), per geometry
+  double *lo;     // per molecule: FP32 copies of the L^-1 buffer and of H0p
+                  // (2 n^2 floats inside the n^2-double block)
   double *ldiag;  // diagonal of the Cholesky factor L (per AO)
   double *invit;  // 5 * nmat: inverse-iteration LU factors
   // per AO
@@ -75,6 +77,7 @@ struct Work {
   double *cn, *erep, *qat, *grad, *dedcn;  // grad: [natom][3]
   // per molecule
   int32_t *status, *phase, *iter, *kvec, *nhist;
+  int32_t *prec;    // 0: the next pass runs in FP32, 1: in FP64
   double *efermi;   // [2][nmol]
   double *energy;   // [nmol][6]: total, rep, h0, es2, es3, fermi
   double *resid;    // [nmol][2]: L2, max norm of the last potential change
@@ -97,6 +100,12 @@ __device__ __forceinline__ double warp_max(double v) {
   return v;
 }
 
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
 __device__ __forceinline__ int warp_sum_int(int v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -116,6 +125,22 @@ __device__ __forceinline__ double block_sum(double v, double *red) {
   if (threadIdx.x == 0) red[0] = t;
   __syncthreads();
   double r = red[0];
+  __syncthreads();
+  return r;
+}
+
+// Block-wide FP32 sum (same contract as the FP64 one).
+__device__ __forceinline__ float block_sum(float v, float *red) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  float t = (threadIdx.x < nw) ? red[threadIdx.x] : 0.0f;
+  if (wid == 0) t = warp_sum(t);
+  if (threadIdx.x == 0) red[0] = t;
+  __syncthreads();
+  float r = red[0];
   __syncthreads();
   return r;
 }

@@ -22,6 +22,18 @@
 //     cluster), only for orbitals with non-zero Fermi occupation;
 //   * back-transformation: each thread owns one eigenvector column and
 //     applies all Householder reflectors to it.
+//
+// Mixed precision.  GB300 retires 64 FP32 FMAs for every FP64 FMA, so the
+// early SCF passes of a molecule (potential change above ~1e-5) run the
+// per-pass linear algebra (Fock transform, tridiagonalisation, bisection,
+// inverse iteration, back-transformation, density) in FP32; the passes that
+// decide convergence, and the final pass that defines the energy, charges
+// and forces, run in FP64.  Every kernel of that chain is a template on the
+// scalar type; a molecule's w.prec flag selects the instantiation per block
+// (block-uniform branch, one launch per stage).  FP32 operands live in the
+// same per-molecule blocks as the FP64 ones (n x n floats at the start of
+// the n x n double block); FP32 copies of L^-1 (with L^T above the
+// diagonal) and of L^-1 H0 L^-T are made once per geometry in w.lo.
 #include "internal.cuh"
 
 #include <cmath>
@@ -35,6 +47,40 @@ namespace {
 
 constexpr double kEps = 2.220446049250313e-16;
 constexpr double kSafeMin = 2.2250738585072014e-308;
+
+// Per-type constants of the templated kernels.
+template <typename T> struct Num;
+template <> struct Num<double> {
+  static constexpr double eps = 2.220446049250313e-16;
+  static constexpr double safemin = 2.2250738585072014e-308;
+  static constexpr double ctol = 1e-4;   // relative width of an eigenvalue cluster
+};
+template <> struct Num<float> {
+  static constexpr double eps = 1.1920928955078125e-07;
+  static constexpr double safemin = 1.1754943508222875e-38;
+  static constexpr double ctol = 1e-3;
+};
+
+// FP32 or FP64 view of a per-molecule n x n work block.
+template <typename T>
+__device__ __forceinline__ T *mat_view(double *base, int64_t mat0) {
+  return reinterpret_cast<T *>(base + mat0);
+}
+// L^-1 buffer (strict upper triangle: L^T) and L^-1 H0 L^-T in precision T.
+template <typename T> __device__ __forceinline__ const T *linv_view(const Work &w, const MolDesc &md);
+template <> __device__ __forceinline__ const double *linv_view<double>(const Work &w, const MolDesc &md) {
+  return w.Linv + md.mat0;
+}
+template <> __device__ __forceinline__ const float *linv_view<float>(const Work &w, const MolDesc &md) {
+  return reinterpret_cast<const float *>(w.lo + md.mat0);
+}
+template <typename T> __device__ __forceinline__ const T *h0p_view(const Work &w, const MolDesc &md);
+template <> __device__ __forceinline__ const double *h0p_view<double>(const Work &w, const MolDesc &md) {
+  return w.H0p + md.mat0;
+}
+template <> __device__ __forceinline__ const float *h0p_view<float>(const Work &w, const MolDesc &md) {
+  return reinterpret_cast<const float *>(w.lo + md.mat0) + (int64_t)md.nao * md.nao;
+}
 
 __device__ __forceinline__ int find_mol_tile(const MolDesc *mol, const int64_t *tile0, int nmol,
                                              int64_t t) {
@@ -129,17 +175,12 @@ __global__ void __launch_bounds__(512) k_cholesky(DevPlan pl, Work w) {
 // ---------------------------------------------------------------------------
 constexpr int BM = 64, BN = 64, BK = 16;
 
-__global__ void __launch_bounds__(256) k_gemm(DevPlan pl, Work w, const int64_t *tile0, int mode, int all) {
-  const int64_t t = blockIdx.x;
-  const int m = find_mol_tile(pl.mol, tile0, pl.nmol, t);
-  if (!all && w.phase[m] == kPhaseDone) return;
-  const MolDesc md = pl.mol[m];
+// One 64 x 64 output tile of molecule md in precision T (modes 2, 3 and 6
+// run in either precision; the others only in FP64).
+template <typename T>
+__device__ __forceinline__ void gemm_tile(const DevPlan &pl, const Work &w, const MolDesc &md, int mode,
+                                          int i0, int j0, int kvec, T (*sa)[BM + 1], T (*sb)[BN + 1]) {
   const int n = md.nao;
-  const int nt = (n + BN - 1) / BN;
-  const int local = (int)(t - tile0[m]);
-  const int ti = local / nt, tj = local % nt;
-  const int i0 = ti * BM, j0 = tj * BN;
-  const int kvec = min(max(w.kvec[m], 0), n);
   const bool sym = (mode == 1 || mode == 3 || mode == 4 || mode == 5 || mode == 6);
   const int ncol = (mode == 2) ? kvec : n;
   const int K = (mode == 3 || mode == 4) ? kvec : n;
@@ -154,23 +195,21 @@ __global__ void __launch_bounds__(256) k_gemm(DevPlan pl, Work w, const int64_t 
     kmax = min(K, i0 + BM);
   }
 
-  const double *Lv = w.Linv + md.mat0;
+  const T *Lv = linv_view<T>(w, md);
   const double *S = w.S + md.mat0, *H = w.H0 + md.mat0;
-  const double *Zs = w.Z + md.mat0, *As = w.A + md.mat0;
+  const T *Zs = mat_view<T>(w.Z, md.mat0), *As = mat_view<T>(w.A, md.mat0);
   const double *occa = w.occ + md.ao0, *occb = w.occ + pl.nao + md.ao0;
   const double *eig = w.eig + md.ao0;
   const int32_t *aosh = pl.ao_sh + md.ao0;
   const double *vin = w.vin;
 
-  __shared__ double sa[BK][BM + 1];
-  __shared__ double sb[BK][BN + 1];
   const int tid = threadIdx.x;
   const int tx = tid & 15, ty = tid >> 4;
-  double acc[4][4];
+  T acc[4][4];
 #pragma unroll
   for (int a = 0; a < 4; ++a)
 #pragma unroll
-    for (int b = 0; b < 4; ++b) acc[a][b] = 0.0;
+    for (int b = 0; b < 4; ++b) acc[a][b] = T(0);
 
   for (int k0 = kmin; k0 < kmax; k0 += BK) {
     // A tile: sa[kk][ii] = A(i0+ii, k0+kk)
@@ -180,13 +219,13 @@ __global__ void __launch_bounds__(256) k_gemm(DevPlan pl, Work w, const int64_t 
       int ii, kk;
       if (mode == 2) { kk = e >> 6; ii = e & 63; } else { ii = e >> 4; kk = e & 15; }
       const int i = i0 + ii, k = k0 + kk;
-      double v = 0.0;
+      T v = T(0);
       if (i < n && k < K) {
         switch (mode) {
-          case 0: v = (k <= i) ? Lv[(int64_t)i * n + k] : 0.0; break;
+          case 0: v = (k <= i) ? Lv[(int64_t)i * n + k] : T(0); break;
           case 1: case 5: v = Zs[(int64_t)i * n + k]; break;
-          case 2: v = (k >= i) ? Lv[(int64_t)k * n + i] : 0.0; break;
-          case 6: v = (k <= i) ? Lv[(int64_t)i * n + k] * vin[aosh[k]] : 0.0; break;
+          case 2: v = (k >= i) ? Lv[(int64_t)k * n + i] : T(0); break;
+          case 6: v = (k <= i) ? Lv[(int64_t)i * n + k] * (T)vin[aosh[k]] : T(0); break;
           default: v = As[(int64_t)i * n + k]; break;
         }
       }
@@ -199,21 +238,21 @@ __global__ void __launch_bounds__(256) k_gemm(DevPlan pl, Work w, const int64_t 
       int jj, kk;
       if (mode == 0 || mode == 2) { kk = e >> 6; jj = e & 63; } else { jj = e >> 4; kk = e & 15; }
       const int j = j0 + jj, k = k0 + kk;
-      double v = 0.0;
+      T v = T(0);
       if (j < ncol && k < K) {
         switch (mode) {
           case 0: {
             const int64_t idx = (int64_t)k * n + j;
-            v = H[idx] - 0.5 * S[idx] * (vin[aosh[k]] + vin[aosh[j]]);
+            v = (T)(H[idx] - 0.5 * S[idx] * (vin[aosh[k]] + vin[aosh[j]]));
             break;
           }
-          case 1: case 5: v = (k <= j) ? Lv[(int64_t)j * n + k] : 0.0; break;
+          case 1: case 5: v = (k <= j) ? Lv[(int64_t)j * n + k] : T(0); break;
           case 2: v = Zs[(int64_t)k * n + j]; break;
           case 6:  // L(k, j): stored transposed above the diagonal
-            v = (k > j) ? Lv[(int64_t)j * n + k] : ((k == j) ? w.ldiag[md.ao0 + j] : 0.0);
+            v = (k > j) ? Lv[(int64_t)j * n + k] : ((k == j) ? (T)w.ldiag[md.ao0 + j] : T(0));
             break;
-          case 3: v = As[(int64_t)j * n + k] * (occa[k] + occb[k]); break;
-          default: v = As[(int64_t)j * n + k] * (occa[k] + occb[k]) * eig[k]; break;
+          case 3: v = As[(int64_t)j * n + k] * (T)(occa[k] + occb[k]); break;
+          default: v = As[(int64_t)j * n + k] * (T)((occa[k] + occb[k]) * eig[k]); break;
         }
       }
       sb[kk][jj] = v;
@@ -221,7 +260,7 @@ __global__ void __launch_bounds__(256) k_gemm(DevPlan pl, Work w, const int64_t 
     __syncthreads();
 #pragma unroll
     for (int kk = 0; kk < BK; ++kk) {
-      double a[4], b[4];
+      T a[4], b[4];
 #pragma unroll
       for (int r = 0; r < 4; ++r) a[r] = sa[kk][ty * 4 + r];
 #pragma unroll
@@ -233,17 +272,18 @@ __global__ void __launch_bounds__(256) k_gemm(DevPlan pl, Work w, const int64_t 
     }
     __syncthreads();
   }
-  double *C;
+  T *C = nullptr;
+  double *Pd = w.P + md.mat0;  // the density is always stored in FP64
   switch (mode) {
-    case 0: C = w.Z + md.mat0; break;
-    case 1: C = w.A + md.mat0; break;
-    case 2: C = w.A + md.mat0; break;
-    case 3: C = w.P + md.mat0; break;
-    case 5: C = w.H0p + md.mat0; break;
-    case 6: C = w.A + md.mat0; break;
-    default: C = w.Z + md.mat0; break;
+    case 0: C = mat_view<T>(w.Z, md.mat0); break;
+    case 1: C = mat_view<T>(w.A, md.mat0); break;
+    case 2: C = mat_view<T>(w.A, md.mat0); break;
+    case 3: break;
+    case 5: C = mat_view<T>(w.H0p, md.mat0); break;
+    case 6: C = mat_view<T>(w.A, md.mat0); break;
+    default: C = mat_view<T>(w.Z, md.mat0); break;
   }
-  const double *H0p = w.H0p + md.mat0;
+  const T *H0p = h0p_view<T>(w, md);
 #pragma unroll
   for (int r = 0; r < 4; ++r) {
     const int i = i0 + ty * 4 + r;
@@ -254,14 +294,52 @@ __global__ void __launch_bounds__(256) k_gemm(DevPlan pl, Work w, const int64_t 
       if (j >= ncol) continue;
       if (sym) {
         if (j > i) continue;
-        double val = acc[r][c];
-        if (mode == 6) val = H0p[(int64_t)i * n + j] - ((i == j) ? val : 0.5 * val);
-        C[(int64_t)i * n + j] = val;
-        C[(int64_t)j * n + i] = val;
+        T val = acc[r][c];
+        if (mode == 6) val = H0p[(int64_t)i * n + j] - ((i == j) ? val : T(0.5) * val);
+        if (mode == 3) {
+          Pd[(int64_t)i * n + j] = (double)val;
+          Pd[(int64_t)j * n + i] = (double)val;
+        } else {
+          C[(int64_t)i * n + j] = val;
+          C[(int64_t)j * n + i] = val;
+        }
       } else {
         C[(int64_t)i * n + j] = acc[r][c];
       }
     }
+  }
+}
+
+__global__ void __launch_bounds__(256) k_gemm(DevPlan pl, Work w, const int64_t *tile0, int mode, int all) {
+  const int64_t t = blockIdx.x;
+  const int m = find_mol_tile(pl.mol, tile0, pl.nmol, t);
+  if (!all && w.phase[m] == kPhaseDone) return;
+  const MolDesc md = pl.mol[m];
+  const int n = md.nao;
+  const int nt = (n + BN - 1) / BN;
+  const int local = (int)(t - tile0[m]);
+  const int ti = local / nt, tj = local % nt;
+  const int kvec = min(max(w.kvec[m], 0), n);
+  __shared__ double sa[BK][BM + 1];
+  __shared__ double sb[BK][BN + 1];
+  const bool lowp = (mode == 2 || mode == 3 || mode == 6) && w.prec[m] == 0;
+  if (lowp)
+    gemm_tile<float>(pl, w, md, mode, ti * BM, tj * BN, kvec, reinterpret_cast<float (*)[BM + 1]>(&sa[0][0]),
+                     reinterpret_cast<float (*)[BN + 1]>(&sb[0][0]));
+  else
+    gemm_tile<double>(pl, w, md, mode, ti * BM, tj * BN, kvec, sa, sb);
+}
+
+// FP32 copies of the L^-1 buffer (L^-1 below, L^T above the diagonal) and of
+// L^-1 H0 L^-T, once per geometry (one block per molecule).
+__global__ void __launch_bounds__(256) k_lowp_copies(DevPlan pl, Work w) {
+  const MolDesc md = pl.mol[blockIdx.x];
+  const int64_t nn = (int64_t)md.nao * md.nao;
+  float *dst = reinterpret_cast<float *>(w.lo + md.mat0);
+  const double *lv = w.Linv + md.mat0, *hp = w.H0p + md.mat0;
+  for (int64_t e = threadIdx.x; e < nn; e += blockDim.x) {
+    dst[e] = (float)lv[e];
+    dst[nn + e] = (float)hp[e];
   }
 }
 
@@ -272,52 +350,48 @@ __global__ void __launch_bounds__(256) k_gemm(DevPlan pl, Work w, const int64_t 
 // ---------------------------------------------------------------------------
 constexpr int kTrdThreads = 512;
 
-__global__ void __launch_bounds__(kTrdThreads) k_tridiag(DevPlan pl, Work w) {
-  const int m = blockIdx.x;
-  if (w.phase[m] == kPhaseDone) return;
-  const MolDesc md = pl.mol[m];
+template <typename T>
+__device__ __forceinline__ void tridiag_body(const MolDesc &md, const Work &w, T *sm, T *red) {
   const int n = md.nao;
-  double *A = w.A + md.mat0;
+  T *A = mat_view<T>(w.A, md.mat0);
   double *d = w.d + md.ao0, *e = w.e + md.ao0, *tau = w.tau + md.ao0;
-  extern __shared__ double sm[];
-  double *vs = sm;          // [n]
-  double *ps = sm + n;      // [n]
-  __shared__ double red[32];
-  __shared__ double sc[4];
+  T *vs = sm;          // [n]
+  T *ps = sm + n;      // [n]
+  __shared__ T sc[4];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int k = 0; k + 2 < n; ++k) {
     const int m1 = n - k - 1;  // length of x
     // column x = A[k+1.., k]
-    double part = 0.0;
+    T part = T(0);
     for (int t = 1 + threadIdx.x; t < m1; t += blockDim.x) {
-      const double x = A[(int64_t)(k + 1 + t) * n + k];
+      const T x = A[(int64_t)(k + 1 + t) * n + k];
       part += x * x;
     }
-    const double xn2 = block_sum(part, red);
+    const T xn2 = block_sum(part, red);
     if (threadIdx.x == 0) {
-      const double alpha = A[(int64_t)(k + 1) * n + k];
+      const T alpha = A[(int64_t)(k + 1) * n + k];
       d[k] = A[(int64_t)k * n + k];
-      if (xn2 == 0.0) {
-        sc[0] = 0.0;      // tau
-        sc[1] = 0.0;      // scale
+      if (xn2 == T(0)) {
+        sc[0] = T(0);      // tau
+        sc[1] = T(0);      // scale
         e[k] = alpha;
       } else {
-        const double beta = -copysign(sqrt(alpha * alpha + xn2), alpha);
+        const T beta = -copysign(sqrt(alpha * alpha + xn2), alpha);
         sc[0] = (beta - alpha) / beta;
-        sc[1] = 1.0 / (alpha - beta);
+        sc[1] = T(1) / (alpha - beta);
         e[k] = beta;
       }
       tau[k] = sc[0];
     }
     __syncthreads();
-    const double tk = sc[0], scale = sc[1];
-    if (tk == 0.0) {
+    const T tk = sc[0], scale = sc[1];
+    if (tk == T(0)) {
       // no reflection needed (tau = 0 makes the stored vector irrelevant)
       __syncthreads();
       continue;
     }
     for (int t = threadIdx.x; t < m1; t += blockDim.x) {
-      double v = (t == 0) ? 1.0 : A[(int64_t)(k + 1 + t) * n + k] * scale;
+      T v = (t == 0) ? T(1) : A[(int64_t)(k + 1 + t) * n + k] * scale;
       vs[t] = v;
     }
     __syncthreads();
@@ -326,23 +400,23 @@ __global__ void __launch_bounds__(kTrdThreads) k_tridiag(DevPlan pl, Work w) {
     for (int t = threadIdx.x; t < m1; t += blockDim.x) A[(int64_t)k * n + k + 1 + t] = vs[t];
     // p = tau * A22 v   (warp per row)
     for (int i = wid; i < m1; i += nw) {
-      const double *row = A + (int64_t)(k + 1 + i) * n + (k + 1);
-      double s = 0.0;
+      const T *row = A + (int64_t)(k + 1 + i) * n + (k + 1);
+      T s = T(0);
       for (int j = lane; j < m1; j += 32) s += row[j] * vs[j];
       s = warp_sum(s);
       if (lane == 0) ps[i] = tk * s;
     }
     __syncthreads();
-    double pv = 0.0;
+    T pv = T(0);
     for (int t = threadIdx.x; t < m1; t += blockDim.x) pv += ps[t] * vs[t];
-    const double K = block_sum(pv, red);
-    const double half = 0.5 * tk * K;
+    const T K = block_sum(pv, red);
+    const T half = T(0.5) * tk * K;
     for (int t = threadIdx.x; t < m1; t += blockDim.x) ps[t] -= half * vs[t];  // w
     __syncthreads();
     // A22 -= v w^T + w v^T
     for (int i = wid; i < m1; i += nw) {
-      double *row = A + (int64_t)(k + 1 + i) * n + (k + 1);
-      const double vi = vs[i], wi = ps[i];
+      T *row = A + (int64_t)(k + 1 + i) * n + (k + 1);
+      const T vi = vs[i], wi = ps[i];
       for (int j = lane; j < m1; j += 32) row[j] -= vi * ps[j] + wi * vs[j];
     }
     __syncthreads();
@@ -356,6 +430,18 @@ __global__ void __launch_bounds__(kTrdThreads) k_tridiag(DevPlan pl, Work w) {
       d[0] = A[0];
     }
   }
+}
+
+__global__ void __launch_bounds__(kTrdThreads) k_tridiag(DevPlan pl, Work w) {
+  const int m = blockIdx.x;
+  if (w.phase[m] == kPhaseDone) return;
+  const MolDesc md = pl.mol[m];
+  extern __shared__ double sm[];
+  __shared__ double red[32];
+  if (w.prec[m])
+    tridiag_body<double>(md, w, sm, red);
+  else
+    tridiag_body<float>(md, w, reinterpret_cast<float *>(sm), reinterpret_cast<float *>(red));
 }
 
 // ---------------------------------------------------------------------------
@@ -372,108 +458,117 @@ __global__ void __launch_bounds__(kTrdThreads) k_tridiag(DevPlan pl, Work w) {
 constexpr int kClusterSize = 8;
 constexpr int kTrdClThreads = 256;
 
+template <typename T>
+__device__ __forceinline__ T ld_cg(const T *p) {
+  return __ldcg(p);
+}
+
+template <typename T>
+__device__ __forceinline__ void tridiag_cluster_body(cg::cluster_group &cluster, const MolDesc &md,
+                                                     const Work &w, T *sm, T *red, T *kpart) {
+  const int rank = (int)cluster.block_rank();
+  const int n = md.nao;
+  T *A = mat_view<T>(w.A, md.mat0);
+  double *d = w.d + md.ao0, *e = w.e + md.ao0, *tau = w.tau + md.ao0;
+  T *vs = sm;          // [n] full reflector
+  T *ws = sm + n;      // [n] p, then w, for own rows; full w after gather
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int k = 0; k + 2 < n; ++k) {
+    const int m1 = n - k - 1;
+    // column x = A[k+1.., k] (rebuilt redundantly by every CTA)
+    T part = T(0);
+    for (int t = 1 + threadIdx.x; t < m1; t += blockDim.x) {
+      const T x = ld_cg(A + (int64_t)(k + 1 + t) * n + k);
+      part += x * x;
+    }
+    const T xn2 = block_sum(part, red);
+    const T alpha = ld_cg(A + (int64_t)(k + 1) * n + k);
+    T tk = T(0), scale = T(0), beta = alpha;
+    if (xn2 != T(0)) {
+      beta = -copysign(sqrt(alpha * alpha + xn2), alpha);
+      tk = (beta - alpha) / beta;
+      scale = T(1) / (alpha - beta);
+    }
+    if (rank == 0 && threadIdx.x == 0) {
+      d[k] = ld_cg(A + (int64_t)k * n + k);
+      e[k] = beta;
+      tau[k] = tk;
+    }
+    if (tk == T(0)) {
+      cluster.sync();
+      continue;
+    }
+    for (int t = threadIdx.x; t < m1; t += blockDim.x)
+      vs[t] = (t == 0) ? T(1) : ld_cg(A + (int64_t)(k + 1 + t) * n + k) * scale;
+    __syncthreads();
+    if (rank == 0)
+      for (int t = threadIdx.x; t < m1; t += blockDim.x) A[(int64_t)k * n + k + 1 + t] = vs[t];
+    // p = tau A22 v for own rows (warp per row)
+    const int first = (rank - (k + 1) % kClusterSize + kClusterSize) % kClusterSize;
+    T pv = T(0);
+    for (int t0 = wid; ; t0 += nw) {
+      // own rows: global row i = k+1+t with i % C == rank
+      const int t = first + t0 * kClusterSize;
+      if (t >= m1) break;
+      const T *row = A + (int64_t)(k + 1 + t) * n + (k + 1);
+      T sacc = T(0);
+      for (int j = lane; j < m1; j += 32) sacc += ld_cg(row + j) * vs[j];
+      sacc = warp_sum(sacc) * tk;
+      if (lane == 0) {
+        ws[t] = sacc;
+        pv += sacc * vs[t];
+      }
+    }
+    const T kp = block_sum(pv, red);
+    if (threadIdx.x == 0) *kpart = kp;
+    cluster.sync();
+    T K = T(0);
+    for (int r = 0; r < kClusterSize; ++r) K += *cluster.map_shared_rank(kpart, r);
+    const T half = T(0.5) * tk * K;
+    for (int t = first + threadIdx.x * kClusterSize; t < m1; t += blockDim.x * kClusterSize)
+      ws[t] -= half * vs[t];
+    cluster.sync();
+    // gather w of all rows into local shared memory
+    T *wl = sm + 2 * n;  // [n]
+    for (int t = threadIdx.x; t < m1; t += blockDim.x) {
+      const int owner = (k + 1 + t) % kClusterSize;
+      wl[t] = *cluster.map_shared_rank(ws + t, owner);
+    }
+    __syncthreads();
+    // A22 -= v w^T + w v^T on own rows
+    for (int t = first + wid * kClusterSize; t < m1; t += nw * kClusterSize) {
+      T *row = A + (int64_t)(k + 1 + t) * n + (k + 1);
+      const T vi = vs[t], wi = wl[t];
+      for (int j = lane; j < m1; j += 32) row[j] -= vi * wl[j] + wi * vs[j];
+    }
+    cluster.sync();
+  }
+  if (rank == 0 && threadIdx.x == 0) {
+    if (n >= 2) {
+      d[n - 2] = ld_cg(A + (int64_t)(n - 2) * n + (n - 2));
+      d[n - 1] = ld_cg(A + (int64_t)(n - 1) * n + (n - 1));
+      e[n - 2] = ld_cg(A + (int64_t)(n - 1) * n + (n - 2));
+    } else {
+      d[0] = ld_cg(A);
+    }
+  }
+}
+
 __global__ void __cluster_dims__(kClusterSize, 1, 1) __launch_bounds__(kTrdClThreads)
     k_tridiag_cluster(DevPlan pl, Work w, const int32_t *mol_list) {
   cg::cluster_group cluster = cg::this_cluster();
-  const int rank = (int)cluster.block_rank();
   const int m = mol_list[blockIdx.x / kClusterSize];
   const MolDesc md = pl.mol[m];
-  const int n = md.nao;
-  double *A = w.A + md.mat0;
-  double *d = w.d + md.ao0, *e = w.e + md.ao0, *tau = w.tau + md.ao0;
   extern __shared__ double sm[];
-  double *vs = sm;          // [n] full reflector
-  double *ws = sm + n;      // [n] p, then w, for own rows; full w after gather
   __shared__ double red[32];
   __shared__ double kpart;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const bool done = (w.phase[m] == kPhaseDone);  // uniform over the cluster
   if (!done) {
-    for (int k = 0; k + 2 < n; ++k) {
-      const int m1 = n - k - 1;
-      // column x = A[k+1.., k] (rebuilt redundantly by every CTA)
-      double part = 0.0;
-      for (int t = 1 + threadIdx.x; t < m1; t += blockDim.x) {
-        const double x = __ldcg(A + (int64_t)(k + 1 + t) * n + k);
-        part += x * x;
-      }
-      const double xn2 = block_sum(part, red);
-      const double alpha = __ldcg(A + (int64_t)(k + 1) * n + k);
-      double tk = 0.0, scale = 0.0, beta = alpha;
-      if (xn2 != 0.0) {
-        beta = -copysign(sqrt(alpha * alpha + xn2), alpha);
-        tk = (beta - alpha) / beta;
-        scale = 1.0 / (alpha - beta);
-      }
-      if (rank == 0 && threadIdx.x == 0) {
-        d[k] = __ldcg(A + (int64_t)k * n + k);
-        e[k] = beta;
-        tau[k] = tk;
-      }
-      if (tk == 0.0) {
-        cluster.sync();
-        continue;
-      }
-      for (int t = threadIdx.x; t < m1; t += blockDim.x)
-        vs[t] = (t == 0) ? 1.0 : __ldcg(A + (int64_t)(k + 1 + t) * n + k) * scale;
-      __syncthreads();
-      if (rank == 0)
-        for (int t = threadIdx.x; t < m1; t += blockDim.x) A[(int64_t)k * n + k + 1 + t] = vs[t];
-      // p = tau A22 v for own rows (warp per row)
-      double pv = 0.0;
-      for (int t0 = wid; ; t0 += nw) {
-        // own rows: global row i = k+1+t with i % C == rank
-        const int first = (rank - (k + 1) % kClusterSize + kClusterSize) % kClusterSize;
-        const int t = first + t0 * kClusterSize;
-        if (t >= m1) break;
-        const double *row = A + (int64_t)(k + 1 + t) * n + (k + 1);
-        double sacc = 0.0;
-        for (int j = lane; j < m1; j += 32) sacc += __ldcg(row + j) * vs[j];
-        sacc = warp_sum(sacc) * tk;
-        if (lane == 0) {
-          ws[t] = sacc;
-          pv += sacc * vs[t];
-        }
-      }
-      const double kp = block_sum(pv, red);
-      if (threadIdx.x == 0) kpart = kp;
-      cluster.sync();
-      double K = 0.0;
-      for (int r = 0; r < kClusterSize; ++r) K += *cluster.map_shared_rank(&kpart, r);
-      const double half = 0.5 * tk * K;
-      {
-        const int first = (rank - (k + 1) % kClusterSize + kClusterSize) % kClusterSize;
-        for (int t = first + threadIdx.x * kClusterSize; t < m1; t += blockDim.x * kClusterSize)
-          ws[t] -= half * vs[t];
-      }
-      cluster.sync();
-      // gather w of all rows into local shared memory
-      double *wl = sm + 2 * n;  // [n]
-      for (int t = threadIdx.x; t < m1; t += blockDim.x) {
-        const int owner = (k + 1 + t) % kClusterSize;
-        wl[t] = *cluster.map_shared_rank(ws + t, owner);
-      }
-      __syncthreads();
-      // A22 -= v w^T + w v^T on own rows
-      {
-        const int first = (rank - (k + 1) % kClusterSize + kClusterSize) % kClusterSize;
-        for (int t = first + wid * kClusterSize; t < m1; t += nw * kClusterSize) {
-          double *row = A + (int64_t)(k + 1 + t) * n + (k + 1);
-          const double vi = vs[t], wi = wl[t];
-          for (int j = lane; j < m1; j += 32) row[j] -= vi * wl[j] + wi * vs[j];
-        }
-      }
-      cluster.sync();
-    }
-    if (rank == 0 && threadIdx.x == 0) {
-      if (n >= 2) {
-        d[n - 2] = __ldcg(A + (int64_t)(n - 2) * n + (n - 2));
-        d[n - 1] = __ldcg(A + (int64_t)(n - 1) * n + (n - 1));
-        e[n - 2] = __ldcg(A + (int64_t)(n - 1) * n + (n - 2));
-      } else {
-        d[0] = __ldcg(A);
-      }
-    }
+    if (w.prec[m])
+      tridiag_cluster_body<double>(cluster, md, w, sm, red, &kpart);
+    else
+      tridiag_cluster_body<float>(cluster, md, w, reinterpret_cast<float *>(sm),
+                                  reinterpret_cast<float *>(red), reinterpret_cast<float *>(&kpart));
   }
   cluster.sync();
 }
@@ -523,37 +618,66 @@ __device__ __forceinline__ int sturm_count(const double *ds, const double *e2, i
   return cnt;
 }
 
+// FP32 form of the same recurrence (FP32 passes): |d - x| and e^2 stay
+// below 2^20 for xTB Hamiltonians in Hartree, so rescaling by 2^+-40 keeps
+// every minor inside the FP32 range.
+__device__ __forceinline__ int sturm_count(const float *ds, const float *e2, int n, float x,
+                                           float pivmin) {
+  float pm = 1.0f;
+  float pc = ds[0] - x;
+  if (pc == 0.0f) pc = -pivmin;
+  int cnt = (int)((unsigned)__float_as_int(pc) >> 31);
+  for (int j = 1; j < n; ++j) {
+    float pn = fmaf(ds[j] - x, pc, -e2[j - 1] * pm);
+    const int bits = __float_as_int(pn);
+    const int bc = __float_as_int(pc);
+    if (pn == 0.0f) pn = (bc < 0) ? pivmin : -pivmin;
+    const int bn = __float_as_int(pn);
+    cnt += (int)((unsigned)(bn ^ bc) >> 31);
+    const int ex = (bits >> 23) & 0xff;
+    pm = pc;
+    pc = pn;
+    if (ex > 127 + 40) {
+      pm *= 0x1p-40f;
+      pc *= 0x1p-40f;
+    } else if (ex < 127 - 40) {
+      const int exm = (__float_as_int(pm) >> 23) & 0xff;
+      if (exm < 127 - 20) {
+        pm *= 0x1p+40f;
+        pc *= 0x1p+40f;
+      }
+    }
+  }
+  return cnt;
+}
+
 constexpr int kBisectSplit = 4;
 
-__global__ void __launch_bounds__(256) k_bisect(DevPlan pl, Work w, double kt) {
-  const int m = blockIdx.x;
-  const int part = blockIdx.y;  // eigenvalue indices part, part + split, ...
-  if (w.phase[m] == kPhaseDone) return;
-  const MolDesc md = pl.mol[m];
+template <typename T>
+__device__ __forceinline__ void bisect_body(const MolDesc &md, const Work &w, int part, double kt, T *sm,
+                                            double *red) {
   const int n = md.nao;
-  extern __shared__ double sm[];
-  double *ds = sm, *e2 = sm + n;
-  __shared__ double red[32];
+  T *ds = sm, *e2 = sm + n;
   __shared__ double s_cut;
   const double *d = w.d + md.ao0, *e = w.e + md.ao0;
   double *ev = w.eig + md.ao0;
   double glo = 1e300, ghi = -1e300, emax = 0.0;
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    ds[i] = d[i];
+    ds[i] = (T)d[i];
     const double el = (i > 0) ? fabs(e[i - 1]) : 0.0;
     const double er = (i < n - 1) ? fabs(e[i]) : 0.0;
-    e2[i] = (i < n - 1) ? e[i] * e[i] : 0.0;
+    e2[i] = (i < n - 1) ? (T)(e[i] * e[i]) : T(0);
     glo = fmin(glo, d[i] - el - er);
     ghi = fmax(ghi, d[i] + el + er);
-    emax = fmax(emax, e2[i]);
+    emax = fmax(emax, (i < n - 1) ? e[i] * e[i] : 0.0);
   }
   glo = block_min(glo, red);
   ghi = block_max(ghi, red);
   emax = block_max(emax, red);
   const double tnorm = fmax(fabs(glo), fabs(ghi));
-  glo -= 2.0 * kEps * tnorm * n + 1e-300;
-  ghi += 2.0 * kEps * tnorm * n + 1e-300;
-  const double pivmin = kSafeMin * fmax(1.0, emax);
+  glo -= 2.0 * Num<T>::eps * tnorm * n + 1e-300;
+  ghi += 2.0 * Num<T>::eps * tnorm * n + 1e-300;
+  const T pivmin = (T)(Num<T>::safemin * fmax(1.0, emax));
   // index of the lowest eigenvalue of the alpha channel that is empty at T=0
   const int lumo = min(n - 1, (int)ceil(md.nel[0] - 5.0e-15));
   // pass 1: every eigenvalue of this part to 1e-4, plus (thread 0) the LUMO
@@ -562,40 +686,53 @@ __global__ void __launch_bounds__(256) k_bisect(DevPlan pl, Work w, double kt) {
   //  which the SCF status check turns into an error, never in a hang)
   const int stride = blockDim.x * kBisectSplit;
   if (threadIdx.x == 0) {
-    double lo = glo, hi = ghi;
-    for (int it = 0; it < 96 && hi - lo > 1.0e-4; ++it) {
-      const double mid = 0.5 * (lo + hi);
+    T lo = (T)glo, hi = (T)ghi;
+    for (int it = 0; it < 96 && hi - lo > T(1.0e-4); ++it) {
+      const T mid = T(0.5) * (lo + hi);
       if (sturm_count(ds, e2, n, mid, pivmin) <= lumo) lo = mid; else hi = mid;
     }
-    s_cut = hi + 60.0 * kt + 0.01;
+    s_cut = (double)hi + 60.0 * kt + 0.01;
   }
   for (int idx = part * blockDim.x + threadIdx.x; idx < n; idx += stride) {
-    double lo = glo, hi = ghi;
-    for (int it = 0; it < 96 && hi - lo > 1.0e-4; ++it) {
-      const double mid = 0.5 * (lo + hi);
+    T lo = (T)glo, hi = (T)ghi;
+    for (int it = 0; it < 96 && hi - lo > T(1.0e-4); ++it) {
+      const T mid = T(0.5) * (lo + hi);
       if (sturm_count(ds, e2, n, mid, pivmin) <= idx) lo = mid; else hi = mid;
     }
-    ev[idx] = lo;            // lower bracket
+    ev[idx] = (double)lo;            // lower bracket
   }
   __syncthreads();
   const double cut = s_cut;
   // pass 2: full precision below the cut
   for (int idx = part * blockDim.x + threadIdx.x; idx < n; idx += stride) {
-    double lo = ev[idx];
-    double hi = lo + 1.0e-4;
-    if (lo < cut) {
-      hi = fmin(hi + 1.0e-4, ghi);
+    T lo = (T)ev[idx];
+    T hi = lo + T(1.0e-4);
+    if ((double)lo < cut) {
+      hi = fmin(hi + T(1.0e-4), (T)ghi);
       // re-establish a valid upper bracket
       for (int it = 0; it < 64 && sturm_count(ds, e2, n, hi, pivmin) <= idx; ++it)
-        hi = fmin(hi + 1.0e-3, ghi + 1.0);
+        hi = fmin(hi + T(1.0e-3), (T)(ghi + 1.0));
       for (int it = 0; it < 128; ++it) {
-        const double mid = 0.5 * (lo + hi);
+        const T mid = T(0.5) * (lo + hi);
         if (mid <= lo || mid >= hi) break;
         if (sturm_count(ds, e2, n, mid, pivmin) <= idx) lo = mid; else hi = mid;
       }
     }
-    ev[idx] = 0.5 * (lo + hi);
+    ev[idx] = 0.5 * ((double)lo + (double)hi);
   }
+}
+
+__global__ void __launch_bounds__(256) k_bisect(DevPlan pl, Work w, double kt) {
+  const int m = blockIdx.x;
+  const int part = blockIdx.y;  // eigenvalue indices part, part + split, ...
+  if (w.phase[m] == kPhaseDone) return;
+  const MolDesc md = pl.mol[m];
+  extern __shared__ double sm[];
+  __shared__ double red[32];
+  if (w.prec[m])
+    bisect_body<double>(md, w, part, kt, sm, red);
+  else
+    bisect_body<float>(md, w, part, kt, reinterpret_cast<float *>(sm), red);
 }
 
 // ---------------------------------------------------------------------------
@@ -615,81 +752,81 @@ constexpr int kInvitThreads = 256;
 // T - lambda I (factors kept in global scratch, interleaved over eigenvectors
 // so that the sequential sweeps of neighbouring threads are coalesced) and
 // one inverse-iteration solve.
-__device__ __forceinline__ void invit_factor(int n, int i, double lam, const double *d, const double *e,
-                                             double pert, double *U1, double *U2, double *U3, double *LM,
-                                             double *PV) {
-  double u1 = d[0] - lam;
-  double u2n = (n > 1) ? e[0] : 0.0;
+template <typename T>
+__device__ __forceinline__ void invit_factor(int n, int i, T lam, const T *d, const T *e, T pert, T *U1,
+                                             T *U2, T *U3, T *LM, T *PV) {
+  T u1 = d[0] - lam;
+  T u2n = (n > 1) ? e[0] : T(0);
   for (int j = 0; j < n - 1; ++j) {
-    const double sub = e[j];
-    const double dn = d[j + 1] - lam;
-    const double sup2 = (j + 1 < n - 1) ? e[j + 1] : 0.0;
+    const T sub = e[j];
+    const T dn = d[j + 1] - lam;
+    const T sup2 = (j + 1 < n - 1) ? e[j + 1] : T(0);
     const int64_t o = (int64_t)j * n + i;
     if (fabs(u1) >= fabs(sub)) {
-      const double mult = (u1 != 0.0) ? sub / u1 : 0.0;
-      U1[o] = (fabs(u1) < pert) ? ((u1 < 0.0) ? -pert : pert) : u1;
+      const T mult = (u1 != T(0)) ? sub / u1 : T(0);
+      U1[o] = (fabs(u1) < pert) ? ((u1 < T(0)) ? -pert : pert) : u1;
       U2[o] = u2n;
-      U3[o] = 0.0;
+      U3[o] = T(0);
       LM[o] = mult;
-      PV[o] = 0.0;
+      PV[o] = T(0);
       u1 = dn - mult * u2n;
       u2n = sup2;
     } else {
-      const double mult = u1 / sub;
+      const T mult = u1 / sub;
       U1[o] = sub;
       U2[o] = dn;
       U3[o] = sup2;
       LM[o] = mult;
-      PV[o] = 1.0;
+      PV[o] = T(1);
       u1 = u2n - mult * dn;
       u2n = -mult * sup2;
     }
   }
   const int64_t o = (int64_t)(n - 1) * n + i;
-  U1[o] = (fabs(u1) < pert) ? ((u1 < 0.0) ? -pert : pert) : u1;
-  U2[o] = 0.0;
-  U3[o] = 0.0;
+  U1[o] = (fabs(u1) < pert) ? ((u1 < T(0)) ? -pert : pert) : u1;
+  U2[o] = T(0);
+  U3[o] = T(0);
 }
 
-__device__ __forceinline__ void invit_solve(int n, int i, const double *U1, const double *U2,
-                                            const double *U3, const double *LM, const double *PV,
-                                            double *Y) {
+template <typename T>
+__device__ __forceinline__ void invit_solve(int n, int i, const T *U1, const T *U2, const T *U3, const T *LM,
+                                            const T *PV, T *Y) {
   for (int j = 0; j < n - 1; ++j) {
     const int64_t o = (int64_t)j * n + i;
-    const double yj = Y[o], yj1 = Y[o + n];
-    const double l = LM[o];
-    if (PV[o] != 0.0) {
+    const T yj = Y[o], yj1 = Y[o + n];
+    const T l = LM[o];
+    if (PV[o] != T(0)) {
       Y[o] = yj1;
       Y[o + n] = yj - l * yj1;
     } else {
       Y[o + n] = yj1 - l * yj;
     }
   }
-  double x1 = 0.0, x2 = 0.0, nrm = 0.0;
+  T x1 = T(0), x2 = T(0), nrm = T(0);
   for (int j = n - 1; j >= 0; --j) {
     const int64_t o = (int64_t)j * n + i;
-    const double s = (Y[o] - U2[o] * x1 - U3[o] * x2) / U1[o];
+    const T s = (Y[o] - U2[o] * x1 - U3[o] * x2) / U1[o];
     Y[o] = s;
     x2 = x1;
     x1 = s;
     nrm = fmax(nrm, fabs(s));
   }
-  const double inv = (nrm > 0.0) ? 1.0 / nrm : 1.0;
-  double s2 = 0.0;
+  const T inv = (nrm > T(0)) ? T(1) / nrm : T(1);
+  T s2 = T(0);
   for (int j = 0; j < n; ++j) {
     const int64_t o = (int64_t)j * n + i;
-    const double y = Y[o] * inv;
+    const T y = Y[o] * inv;
     Y[o] = y;
     s2 += y * y;
   }
-  const double in2 = 1.0 / sqrt(s2);
+  const T in2 = T(1) / sqrt(s2);
   for (int j = 0; j < n; ++j) Y[(int64_t)j * n + i] *= in2;
 }
 
 // Modified Gram-Schmidt inside every cluster of close eigenvalues, one warp
 // per cluster, lanes over vector components.
-__device__ __forceinline__ void invit_cluster_mgs(int n, int kvec, const double *ev, double ctol,
-                                                  double *Y) {
+template <typename T>
+__device__ __forceinline__ void invit_cluster_mgs(int n, int kvec, const double *ev, double ctol, T *Y) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int c = wid; c < kvec; c += nw) {
     if (c > 0 && ev[c] - ev[c - 1] <= ctol) continue;  // not a cluster start
@@ -697,76 +834,122 @@ __device__ __forceinline__ void invit_cluster_mgs(int n, int kvec, const double 
     while (cend < kvec && ev[cend] - ev[cend - 1] <= ctol) ++cend;
     for (int i = c + 1; i < cend; ++i) {
       for (int p = c; p < i; ++p) {
-        double dot = 0.0;
+        T dot = T(0);
         for (int j = lane; j < n; j += 32) dot += Y[(int64_t)j * n + p] * Y[(int64_t)j * n + i];
         dot = warp_sum(dot);
         for (int j = lane; j < n; j += 32) Y[(int64_t)j * n + i] -= dot * Y[(int64_t)j * n + p];
       }
-      double s2 = 0.0;
+      T s2 = T(0);
       for (int j = lane; j < n; j += 32) {
-        const double y = Y[(int64_t)j * n + i];
+        const T y = Y[(int64_t)j * n + i];
         s2 += y * y;
       }
       s2 = warp_sum(s2);
-      const double in2 = 1.0 / sqrt(s2);
+      const T in2 = T(1) / sqrt(s2);
       for (int j = lane; j < n; j += 32) Y[(int64_t)j * n + i] *= in2;
     }
   }
+}
+
+template <typename T>
+__device__ __forceinline__ void invit_body(const MolDesc &md, const Work &w, T *sm, double *red) {
+  const int n = md.nao;
+  const int m = blockIdx.x;
+  const int kvec = min(max(w.kvec[m], 0), n);
+  T *d = sm, *e = sm + n;
+  const double *ev = w.eig + md.ao0;
+  T *Y = mat_view<T>(w.Z, md.mat0);
+  T *U1 = reinterpret_cast<T *>(w.invit + md.mat0 * 5);
+  T *U2 = U1 + (int64_t)n * n;
+  T *U3 = U2 + (int64_t)n * n;
+  T *LM = U3 + (int64_t)n * n;
+  T *PV = LM + (int64_t)n * n;
+  double tl = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    d[i] = (T)w.d[md.ao0 + i];
+    e[i] = (i < n - 1) ? (T)w.e[md.ao0 + i] : T(0);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double el = (i > 0) ? fabs((double)e[i - 1]) : 0.0;
+    const double er = (i < n - 1) ? fabs((double)e[i]) : 0.0;
+    tl = fmax(tl, fabs((double)d[i]) + el + er);
+  }
+  const double tnorm = block_max(tl, red);
+  // eigenvalues closer than ctol |T| are orthogonalised explicitly; others
+  // come out orthogonal to eps |T| / gap from inverse iteration
+  // (FP64: <= 2e-12; FP32: <= 1e-4, enough for the early SCF passes)
+  const double ctol = Num<T>::ctol * tnorm;
+  const T pert = (T)(Num<T>::eps * tnorm);
+  for (int i = threadIdx.x; i < kvec; i += blockDim.x) {
+    invit_factor<T>(n, i, (T)ev[i], d, e, pert, U1, U2, U3, LM, PV);
+    for (int j = 0; j < n; ++j) Y[(int64_t)j * n + i] = (T)start_value(i, j);
+    invit_solve<T>(n, i, U1, U2, U3, LM, PV, Y);
+  }
+  __syncthreads();
+  invit_cluster_mgs<T>(n, kvec, ev, ctol, Y);
+  __syncthreads();
+  for (int i = threadIdx.x; i < kvec; i += blockDim.x) invit_solve<T>(n, i, U1, U2, U3, LM, PV, Y);
+  __syncthreads();
+  invit_cluster_mgs<T>(n, kvec, ev, ctol, Y);
 }
 
 __global__ void __launch_bounds__(kInvitThreads) k_invit(DevPlan pl, Work w) {
   const int m = blockIdx.x;
   if (w.phase[m] == kPhaseDone) return;
   const MolDesc md = pl.mol[m];
-  const int n = md.nao;
-  const int kvec = min(max(w.kvec[m], 0), n);
   extern __shared__ double sm[];
-  double *d = sm, *e = sm + n;
-  const double *ev = w.eig + md.ao0;
-  double *Y = w.Z + md.mat0;
-  double *U1 = w.invit + md.mat0 * 5;
-  double *U2 = U1 + (int64_t)n * n;
-  double *U3 = U2 + (int64_t)n * n;
-  double *LM = U3 + (int64_t)n * n;
-  double *PV = LM + (int64_t)n * n;
   __shared__ double red[32];
-  double tl = 0.0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    d[i] = w.d[md.ao0 + i];
-    e[i] = (i < n - 1) ? w.e[md.ao0 + i] : 0.0;
-  }
-  __syncthreads();
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    const double el = (i > 0) ? fabs(e[i - 1]) : 0.0;
-    const double er = (i < n - 1) ? fabs(e[i]) : 0.0;
-    tl = fmax(tl, fabs(d[i]) + el + er);
-  }
-  const double tnorm = block_max(tl, red);
-  // eigenvalues closer than 1e-4 |T| are orthogonalised explicitly; others
-  // come out orthogonal to eps |T| / gap <= 2e-12 from inverse iteration
-  const double ctol = 1e-4 * tnorm;
-  const double pert = kEps * tnorm;
-  for (int i = threadIdx.x; i < kvec; i += blockDim.x) {
-    invit_factor(n, i, ev[i], d, e, pert, U1, U2, U3, LM, PV);
-    for (int j = 0; j < n; ++j) Y[(int64_t)j * n + i] = start_value(i, j);
-    invit_solve(n, i, U1, U2, U3, LM, PV, Y);
-  }
-  __syncthreads();
-  invit_cluster_mgs(n, kvec, ev, ctol, Y);
-  __syncthreads();
-  for (int i = threadIdx.x; i < kvec; i += blockDim.x) invit_solve(n, i, U1, U2, U3, LM, PV, Y);
-  __syncthreads();
-  invit_cluster_mgs(n, kvec, ev, ctol, Y);
+  if (w.prec[m])
+    invit_body<double>(md, w, sm, red);
+  else
+    invit_body<float>(md, w, reinterpret_cast<float *>(sm), red);
 }
 
 // ---------------------------------------------------------------------------
 // back-transformation Y <- Q Y, Q = H_0 ... H_{n-3}
 // A block owns 32 eigenvector columns and splits the rows over 8 warps:
 // per reflector, partial dot products per warp, one reduction in shared
-// memory, then every warp updates its rows (coalesced 256-byte rows of Y).
+// memory, then every warp updates its rows (coalesced rows of Y).
 // ---------------------------------------------------------------------------
 constexpr int kBtCols = 32;
 constexpr int kBtGroups = 8;
+
+template <typename T>
+__device__ __forceinline__ void backtransform_body(const MolDesc &md, const Work &w, int kvec, int c0, T *vsm,
+                                                   T (*part)[kBtCols], T *sfac) {
+  const int n = md.nao;
+  const T *A = mat_view<T>(w.A, md.mat0);
+  const double *tau = w.tau + md.ao0;
+  T *Y = mat_view<T>(w.Z, md.mat0);
+  const int col = threadIdx.x & (kBtCols - 1), rg = threadIdx.x / kBtCols;
+  const int c = c0 + col;
+  const bool active = c < kvec;
+  for (int k = n - 3; k >= 0; --k) {
+    const T tk = (T)tau[k];
+    if (tk == T(0)) continue;  // uniform across the block
+    const int m1 = n - k - 1;
+    for (int t = threadIdx.x; t < m1; t += blockDim.x) vsm[t] = A[(int64_t)k * n + k + 1 + t];
+    __syncthreads();
+    T s = T(0);
+    if (active)
+      for (int r = rg; r < m1; r += kBtGroups) s += vsm[r] * Y[(int64_t)(k + 1 + r) * n + c];
+    part[rg][col] = s;
+    __syncthreads();
+    if (rg == 0) {
+      T t = T(0);
+#pragma unroll
+      for (int g = 0; g < kBtGroups; ++g) t += part[g][col];
+      sfac[col] = t * tk;
+    }
+    __syncthreads();
+    if (active) {
+      const T f = sfac[col];
+      for (int r = rg; r < m1; r += kBtGroups) Y[(int64_t)(k + 1 + r) * n + c] -= f * vsm[r];
+    }
+    __syncthreads();
+  }
+}
 
 __global__ void __launch_bounds__(kBtCols * kBtGroups) k_backtransform(DevPlan pl, Work w) {
   const int m = blockIdx.y;
@@ -776,39 +959,15 @@ __global__ void __launch_bounds__(kBtCols * kBtGroups) k_backtransform(DevPlan p
   const int kvec = min(max(w.kvec[m], 0), n);
   const int c0 = blockIdx.x * kBtCols;
   if (c0 >= kvec) return;
-  const double *A = w.A + md.mat0;
-  const double *tau = w.tau + md.ao0;
-  double *Y = w.Z + md.mat0;
   extern __shared__ double vsm[];
   __shared__ double part[kBtGroups][kBtCols];
   __shared__ double sfac[kBtCols];
-  const int col = threadIdx.x & (kBtCols - 1), rg = threadIdx.x / kBtCols;
-  const int c = c0 + col;
-  const bool active = c < kvec;
-  for (int k = n - 3; k >= 0; --k) {
-    const double tk = tau[k];
-    if (tk == 0.0) continue;  // uniform across the block
-    const int m1 = n - k - 1;
-    for (int t = threadIdx.x; t < m1; t += blockDim.x) vsm[t] = A[(int64_t)k * n + k + 1 + t];
-    __syncthreads();
-    double s = 0.0;
-    if (active)
-      for (int r = rg; r < m1; r += kBtGroups) s += vsm[r] * Y[(int64_t)(k + 1 + r) * n + c];
-    part[rg][col] = s;
-    __syncthreads();
-    if (rg == 0) {
-      double t = 0.0;
-#pragma unroll
-      for (int g = 0; g < kBtGroups; ++g) t += part[g][col];
-      sfac[col] = t * tk;
-    }
-    __syncthreads();
-    if (active) {
-      const double f = sfac[col];
-      for (int r = rg; r < m1; r += kBtGroups) Y[(int64_t)(k + 1 + r) * n + c] -= f * vsm[r];
-    }
-    __syncthreads();
-  }
+  if (w.prec[m])
+    backtransform_body<double>(md, w, kvec, c0, vsm, part, sfac);
+  else
+    backtransform_body<float>(md, w, kvec, c0, reinterpret_cast<float *>(vsm),
+                              reinterpret_cast<float (*)[kBtCols]>(&part[0][0]),
+                              reinterpret_cast<float *>(sfac));
 }
 
 }  // namespace
@@ -823,6 +982,10 @@ void launch_cholesky(const DevPlan &pl, const Work &w, cudaStream_t s) {
 void launch_gemm(const DevPlan &pl, const Work &w, const int64_t *tile0, int64_t ntile, int mode,
                  int all, cudaStream_t s) {
   if (ntile > 0) k_gemm<<<(unsigned)ntile, 256, 0, s>>>(pl, w, tile0, mode, all);
+}
+
+void launch_lowp_copies(const DevPlan &pl, const Work &w, cudaStream_t s) {
+  k_lowp_copies<<<pl.nmol, 256, 0, s>>>(pl, w);
 }
 
 void launch_tridiag(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s) {

@@ -121,6 +121,10 @@ __device__ __forceinline__ double wdot(const double *a, const double *b, const i
 }
 
 constexpr int kMixThreads = 256;
+// mixed precision: potential change (orbital L2 norm) below which a molecule
+// leaves the FP32 passes, and the most FP32 passes a molecule makes
+constexpr double kLowpSwitch = 1e-4;
+constexpr int kLowpMaxPasses = 40;
 constexpr int kMaxMem = 30;
 
 __global__ void __launch_bounds__(kMixThreads) k_charges_mix(DevParams p, DevPlan pl, Work w, MixOpts o) {
@@ -240,10 +244,15 @@ __global__ void __launch_bounds__(kMixThreads) k_charges_mix(DevParams p, DevPla
   if (threadIdx.x == 0) {
     w.resid[2 * m] = l2;
     w.resid[2 * m + 1] = mx;
+    // an FP32 pass never decides convergence: it hands the molecule to FP64
+    // once the potential change is below kLowpSwitch (or after
+    // kLowpMaxPasses FP32 passes), and before a final pass
+    const bool lowp = (w.prec[m] == 0);
     int flag = 0;
     if (!isfinite(l2)) flag = 3;
-    else if (iter > 0 && l2 < o.x_atol && mx < o.x_atol_max) flag = 1;
+    else if (!lowp && iter > 0 && l2 < o.x_atol && mx < o.x_atol_max) flag = 1;
     else if (iter >= o.maxiter) flag = 2;
+    if (lowp && (flag == 2 || l2 < kLowpSwitch || iter + 1 >= kLowpMaxPasses)) w.prec[m] = 1;
     s_flag = flag;
     if (flag == 3) {
       w.status[m] |= GBXTB_MOL_NONFINITE;

@@ -91,7 +91,10 @@ typedef struct {
   double kt;              /* electronic temperature in Hartree (fermi_etemp * k_B) */
   double broyden_alpha;   /* mixer step */
   int32_t profile;        /* 1: time each kernel class with CUDA events (gbxtb_get_profile) */
-  int32_t reserved;
+  int32_t mixed_precision; /* 1: SCF passes run their linear algebra in FP32 while the
+                              potential change is above 1e-4 (at most 40 passes);
+                              convergence and the final state are always FP64.
+                              0: every pass in FP64 */
 } gbxtb_options;
 
 /* Kernel classes reported by gbxtb_get_profile. */

@@ -191,3 +191,23 @@ def test_charged_and_spin():
         res2 = calc.singlepoint(p, chrg=2.0)
     r2 = go.singlepoint(num, pos, chrg=2.0, mixer="broyden", forces=False)
     assert abs(res2.energy.item() - r2.energy) < 1e-10
+
+
+def test_mixed_precision_same_fixed_point():
+    """The FP32 passes only move the SCF start: with and without them the
+    engine ends on the same fixed point (energies 1e-10 Eh, forces 1e-8)."""
+    mols = molgen.c2_batch(8)
+    num, pos = pad(mols)
+    p = torch.tensor(pos, device="cuda")
+    r64 = calc_for(num, mixed_precision=False).singlepoint(p, forces=True)
+    r32 = calc_for(num, mixed_precision=True).singlepoint(p, forces=True)
+    e64, e32 = r64.energy.cpu().numpy(), r32.energy.cpu().numpy()
+    same = [k for k in range(len(mols)) if same_state(e64[k], e32[k])]
+    assert len(same) >= len(mols) - 1
+    for k in same:
+        assert abs(e64[k] - e32[k]) < 1e-10
+    assert (r64.status == 0).all() and (r32.status == 0).all()
+    g64, g32 = r64.gradient.cpu().numpy(), r32.gradient.cpu().numpy()
+    off = np.concatenate([[0], np.cumsum([len(m[0]) for m in mols])])
+    for k in same:
+        assert np.abs(g64[off[k]:off[k + 1]] - g32[off[k]:off[k + 1]]).max() < 1e-8
