@@ -70,6 +70,7 @@ class Result:
     status: np.ndarray
     iterations: np.ndarray
     shell_potential: np.ndarray | None = None  # final shell-resolved potential (host)
+    fp32_passes: np.ndarray | None = None      # SCF passes per molecule that ran in FP32
 
 
 class _Context:
@@ -286,6 +287,8 @@ class GFN1Calculator:
         status = np.zeros(plan.nmol, dtype=np.int32)
         iters = np.zeros(plan.nmol, dtype=np.int32)
         _lib.check(lib.gbxtb_get_status(plan.handle, _lib.ptr(status, C.c_int32), _lib.ptr(iters, C.c_int32)))
+        p32 = np.zeros(plan.nmol, dtype=np.int32)
+        _lib.check(lib.gbxtb_get_fp32_passes(plan.handle, _lib.ptr(p32, C.c_int32)))
         vsh = np.zeros(int(plan.sizes[2]), dtype=np.float64)
         _lib.check(lib.gbxtb_get_shell_potential(plan.handle, _lib.ptr(vsh, C.c_double)))
         ms = np.zeros(len(_lib.PROF_CLASSES), dtype=np.float64)
@@ -298,7 +301,7 @@ class GFN1Calculator:
                              "total_launches": int(tot.value)}
         self._raise_on_status(status)
         return Result(energy=energy, charges=charges, gradient=grad, status=status, iterations=iters,
-                      shell_potential=vsh)
+                      shell_potential=vsh, fp32_passes=p32)
 
     def _raise_on_status(self, status: np.ndarray) -> None:
         if (status & _lib.MOL_FERMI_FAIL).any():

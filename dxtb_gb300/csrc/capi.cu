@@ -26,9 +26,11 @@ void launch_tridiag(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s);
 void launch_lowp_copies(const DevPlan &pl, const Work &w, cudaStream_t s);
 void launch_tridiag_cluster(const DevPlan &pl, const Work &w, const int32_t *mol_list, int count,
                             int maxn, cudaStream_t s);
-void launch_bisect(const DevPlan &pl, const Work &w, int maxn, double kt, cudaStream_t s);
+void launch_bisect(const DevPlan &pl, const Work &w, int maxn, double kt, const int32_t *mol_list, int count,
+                   int nsplit, cudaStream_t s);
 void launch_invit(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s);
-void launch_backtransform(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s);
+void launch_backtransform(const DevPlan &pl, const Work &w, int maxn, const int32_t *mol_list, int count,
+                          cudaStream_t s);
 cudaError_t set_linalg_smem_limits(int maxn);
 void launch_count_active(const DevPlan &pl, const Work &w, cudaStream_t s);
 }  // namespace gbxtb
@@ -119,7 +121,7 @@ Layout make_layout(const DevPlan &pl) {
   L.add(d * pl.ngam);                                       // gam
   for (int k = 0; k < 4; ++k) L.add(d * pl.natom);          // cn erep qat dedcn
   L.add(d * 3 * pl.natom);                                  // grad
-  for (int k = 0; k < 6; ++k) L.add(i4 * pl.nmol);          // status phase iter kvec nhist prec
+  for (int k = 0; k < 7; ++k) L.add(i4 * pl.nmol);          // status phase iter kvec nhist prec npass32
   L.add(d * 2 * pl.nmol);                                   // efermi
   L.add(d * 6 * pl.nmol);                                   // energy
   L.add(d * 2 * pl.nmol);                                   // resid
@@ -145,6 +147,7 @@ Work make_work(const DevPlan &pl, void *base) {
   w.cn = D(); w.erep = D(); w.qat = D(); w.dedcn = D();
   w.grad = D();
   w.status = I(); w.phase = I(); w.iter = I(); w.kvec = I(); w.nhist = I(); w.prec = I();
+  w.npass32 = I();
   w.efermi = D(); w.energy = D(); w.resid = D();
   w.active = I();
   w.active_list = I();
@@ -500,6 +503,7 @@ int gbxtb_singlepoint(gbxtb_plan *plan, const gbxtb_options *opts, const double 
   CK(cudaMemsetAsync(w.iter, 0, sizeof(int32_t) * pl.nmol, s));
   CK(cudaMemsetAsync(w.kvec, 0, sizeof(int32_t) * pl.nmol, s));
   CK(cudaMemsetAsync(w.nhist, 0, sizeof(int32_t) * pl.nmol, s));
+  CK(cudaMemsetAsync(w.npass32, 0, sizeof(int32_t) * pl.nmol, s));
   // 0: the first passes run in FP32; any non-zero byte pattern means FP64
   CK(cudaMemsetAsync(w.prec, opts->mixed_precision ? 0 : 1, sizeof(int32_t) * pl.nmol, s));
   CK(cudaMemsetAsync(w.vin, 0, sizeof(double) * pl.nsh, s));
@@ -527,14 +531,22 @@ int gbxtb_singlepoint(gbxtb_plan *plan, const gbxtb_options *opts, const double 
     launch_gemm(pl, w, plan->tile0, plan->ntile, 6, 0, s);
     pf.end(GBXTB_PROF_FOCK, 1);
     pf.begin(GBXTB_PROF_TRIDIAG);
-    // fewer molecules than SMs: spread each molecule over a cluster of SMs
-    if (it > 0 && active <= plan->num_sms)
+    // fewer molecules than SMs (the tail of the batch): spread each molecule
+    // over more SMs (an 8-SM cluster for the tridiagonalisation, more blocks
+    // for bisection and back-transformation), working from the device-side
+    // list of molecules still iterating
+    const bool tail = it > 0 && active <= plan->num_sms;
+    if (tail)
       launch_tridiag_cluster(pl, w, w.active_list, active, plan->maxn, s);
     else
       launch_tridiag(pl, w, plan->maxn, s);
     pf.end(GBXTB_PROF_TRIDIAG, 1);
     pf.begin(GBXTB_PROF_BISECT);
-    launch_bisect(pl, w, plan->maxn, opts->kt, s);
+    if (tail)
+      launch_bisect(pl, w, plan->maxn, opts->kt, w.active_list, active,
+                    std::max(4, (4 * plan->num_sms + active - 1) / active), s);
+    else
+      launch_bisect(pl, w, plan->maxn, opts->kt, nullptr, pl.nmol, 4, s);
     pf.end(GBXTB_PROF_BISECT, 1);
     pf.begin(GBXTB_PROF_FERMI);
     launch_fermi(pl, w, opts->kt, opts->fermi_maxiter, s);
@@ -543,7 +555,10 @@ int gbxtb_singlepoint(gbxtb_plan *plan, const gbxtb_options *opts, const double 
     launch_invit(pl, w, plan->maxn, s);
     pf.end(GBXTB_PROF_INVIT, 1);
     pf.begin(GBXTB_PROF_BACKTRANSFORM);
-    launch_backtransform(pl, w, plan->maxn, s);
+    if (tail)
+      launch_backtransform(pl, w, plan->maxn, w.active_list, active, s);
+    else
+      launch_backtransform(pl, w, plan->maxn, nullptr, pl.nmol, s);
     pf.end(GBXTB_PROF_BACKTRANSFORM, 1);
     pf.begin(GBXTB_PROF_DENSITY);
     launch_gemm(pl, w, plan->tile0, plan->ntile, 2, 0, s);
@@ -585,6 +600,13 @@ int gbxtb_get_status(gbxtb_plan *plan, int32_t *status, int32_t *iterations) {
   const int n = plan->pl.nmol;
   if (status) CK(cudaMemcpy(status, plan->last_work.status, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
   if (iterations) CK(cudaMemcpy(iterations, plan->last_work.iter, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+  return GBXTB_OK;
+}
+
+int gbxtb_get_fp32_passes(gbxtb_plan *plan, int32_t *passes) {
+  if (!plan || !plan->has_run || !passes) return fail(GBXTB_ERR_ARG, "no singlepoint has run on this plan");
+  CK(cudaStreamSynchronize(plan->last_stream));
+  CK(cudaMemcpy(passes, plan->last_work.npass32, sizeof(int32_t) * plan->pl.nmol, cudaMemcpyDeviceToHost));
   return GBXTB_OK;
 }
 

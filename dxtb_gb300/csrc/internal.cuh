@@ -78,6 +78,7 @@ struct Work {
   // per molecule
   int32_t *status, *phase, *iter, *kvec, *nhist;
   int32_t *prec;    // 0: the next pass runs in FP32, 1: in FP64
+  int32_t *npass32; // number of FP32 passes the molecule made
   double *efermi;   // [2][nmol]
   double *energy;   // [nmol][6]: total, rep, h0, es2, es3, fermi
   double *resid;    // [nmol][2]: L2, max norm of the last potential change

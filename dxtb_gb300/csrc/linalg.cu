@@ -651,11 +651,10 @@ __device__ __forceinline__ int sturm_count(const float *ds, const float *e2, int
   return cnt;
 }
 
-constexpr int kBisectSplit = 4;
 
 template <typename T>
-__device__ __forceinline__ void bisect_body(const MolDesc &md, const Work &w, int part, double kt, T *sm,
-                                            double *red) {
+__device__ __forceinline__ void bisect_body(const MolDesc &md, const Work &w, int part, int nsplit,
+                                            double kt, T *sm, double *red) {
   const int n = md.nao;
   T *ds = sm, *e2 = sm + n;
   __shared__ double s_cut;
@@ -684,7 +683,7 @@ __device__ __forceinline__ void bisect_body(const MolDesc &md, const Work &w, in
   // bracket that fixes the refinement window
   // (every loop is bounded: a non-finite matrix ends with a garbage value,
   //  which the SCF status check turns into an error, never in a hang)
-  const int stride = blockDim.x * kBisectSplit;
+  const int stride = blockDim.x * nsplit;
   if (threadIdx.x == 0) {
     T lo = (T)glo, hi = (T)ghi;
     for (int it = 0; it < 96 && hi - lo > T(1.0e-4); ++it) {
@@ -722,18 +721,23 @@ __device__ __forceinline__ void bisect_body(const MolDesc &md, const Work &w, in
   }
 }
 
-__global__ void __launch_bounds__(256) k_bisect(DevPlan pl, Work w, double kt) {
-  const int m = blockIdx.x;
-  const int part = blockIdx.y;  // eigenvalue indices part, part + split, ...
+// grid (molecules, parts): block (x, y) handles eigenvalue indices
+// y*256 + t + j*256*parts of molecule mol_list[x] (all molecules if
+// mol_list is null)
+__global__ void __launch_bounds__(256) k_bisect(DevPlan pl, Work w, double kt, const int32_t *mol_list) {
+  const int m = mol_list ? mol_list[blockIdx.x] : (int)blockIdx.x;
+  const int part = blockIdx.y;
   if (w.phase[m] == kPhaseDone) return;
   const MolDesc md = pl.mol[m];
+  if (part * (int)blockDim.x >= md.nao) return;  // no index of this part (uniform)
   extern __shared__ double sm[];
   __shared__ double red[32];
   if (w.prec[m])
-    bisect_body<double>(md, w, part, kt, sm, red);
+    bisect_body<double>(md, w, part, gridDim.y, kt, sm, red);
   else
-    bisect_body<float>(md, w, part, kt, reinterpret_cast<float *>(sm), red);
+    bisect_body<float>(md, w, part, gridDim.y, kt, reinterpret_cast<float *>(sm), red);
 }
+
 
 // ---------------------------------------------------------------------------
 // eigenvectors of the tridiagonal matrix by inverse iteration
@@ -912,17 +916,18 @@ __global__ void __launch_bounds__(kInvitThreads) k_invit(DevPlan pl, Work w) {
 // per reflector, partial dot products per warp, one reduction in shared
 // memory, then every warp updates its rows (coalesced rows of Y).
 // ---------------------------------------------------------------------------
-constexpr int kBtCols = 32;
-constexpr int kBtGroups = 8;
+constexpr int kBtThreads = 256;
 
-template <typename T>
+// COLS eigenvector columns per block, kBtThreads / COLS row groups.
+template <typename T, int COLS>
 __device__ __forceinline__ void backtransform_body(const MolDesc &md, const Work &w, int kvec, int c0, T *vsm,
-                                                   T (*part)[kBtCols], T *sfac) {
+                                                   T *part, T *sfac) {
+  constexpr int kGroups = kBtThreads / COLS;
   const int n = md.nao;
   const T *A = mat_view<T>(w.A, md.mat0);
   const double *tau = w.tau + md.ao0;
   T *Y = mat_view<T>(w.Z, md.mat0);
-  const int col = threadIdx.x & (kBtCols - 1), rg = threadIdx.x / kBtCols;
+  const int col = threadIdx.x % COLS, rg = threadIdx.x / COLS;
   const int c = c0 + col;
   const bool active = c < kvec;
   for (int k = n - 3; k >= 0; --k) {
@@ -933,41 +938,42 @@ __device__ __forceinline__ void backtransform_body(const MolDesc &md, const Work
     __syncthreads();
     T s = T(0);
     if (active)
-      for (int r = rg; r < m1; r += kBtGroups) s += vsm[r] * Y[(int64_t)(k + 1 + r) * n + c];
-    part[rg][col] = s;
+      for (int r = rg; r < m1; r += kGroups) s += vsm[r] * Y[(int64_t)(k + 1 + r) * n + c];
+    part[rg * COLS + col] = s;
     __syncthreads();
     if (rg == 0) {
       T t = T(0);
 #pragma unroll
-      for (int g = 0; g < kBtGroups; ++g) t += part[g][col];
+      for (int g = 0; g < kGroups; ++g) t += part[g * COLS + col];
       sfac[col] = t * tk;
     }
     __syncthreads();
     if (active) {
       const T f = sfac[col];
-      for (int r = rg; r < m1; r += kBtGroups) Y[(int64_t)(k + 1 + r) * n + c] -= f * vsm[r];
+      for (int r = rg; r < m1; r += kGroups) Y[(int64_t)(k + 1 + r) * n + c] -= f * vsm[r];
     }
     __syncthreads();
   }
 }
 
-__global__ void __launch_bounds__(kBtCols * kBtGroups) k_backtransform(DevPlan pl, Work w) {
-  const int m = blockIdx.y;
+// grid (column groups, molecules): molecule mol_list[y] (all if null)
+template <int COLS>
+__global__ void __launch_bounds__(kBtThreads) k_backtransform(DevPlan pl, Work w, const int32_t *mol_list) {
+  const int m = mol_list ? mol_list[blockIdx.y] : (int)blockIdx.y;
   if (w.phase[m] == kPhaseDone) return;
   const MolDesc md = pl.mol[m];
   const int n = md.nao;
   const int kvec = min(max(w.kvec[m], 0), n);
-  const int c0 = blockIdx.x * kBtCols;
+  const int c0 = blockIdx.x * COLS;
   if (c0 >= kvec) return;
   extern __shared__ double vsm[];
-  __shared__ double part[kBtGroups][kBtCols];
-  __shared__ double sfac[kBtCols];
+  __shared__ double part[kBtThreads];
+  __shared__ double sfac[COLS];
   if (w.prec[m])
-    backtransform_body<double>(md, w, kvec, c0, vsm, part, sfac);
+    backtransform_body<double, COLS>(md, w, kvec, c0, vsm, part, sfac);
   else
-    backtransform_body<float>(md, w, kvec, c0, reinterpret_cast<float *>(vsm),
-                              reinterpret_cast<float (*)[kBtCols]>(&part[0][0]),
-                              reinterpret_cast<float *>(sfac));
+    backtransform_body<float, COLS>(md, w, kvec, c0, reinterpret_cast<float *>(vsm),
+                                    reinterpret_cast<float *>(part), reinterpret_cast<float *>(sfac));
 }
 
 }  // namespace
@@ -1001,20 +1007,37 @@ void launch_tridiag_cluster(const DevPlan &pl, const Work &w, const int32_t *mol
   k_tridiag_cluster<<<count * kClusterSize, kTrdClThreads, smem, s>>>(pl, w, mol_list);
 }
 
-void launch_bisect(const DevPlan &pl, const Work &w, int maxn, double kt, cudaStream_t s) {
+// All molecules (mol_list null, count = nmol) or the listed ones; nsplit
+// blocks per molecule.
+void launch_bisect(const DevPlan &pl, const Work &w, int maxn, double kt, const int32_t *mol_list, int count,
+                   int nsplit, cudaStream_t s) {
+  if (count <= 0) return;
   const size_t smem = sizeof(double) * 2 * (size_t)maxn;
-  dim3 grid(pl.nmol, kBisectSplit);
-  k_bisect<<<grid, 256, smem, s>>>(pl, w, kt);
+  const int maxsplit = (maxn + 255) / 256;
+  dim3 grid(count, max(1, min(nsplit, maxsplit)));
+  k_bisect<<<grid, 256, smem, s>>>(pl, w, kt, mol_list);
 }
+
 
 void launch_invit(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s) {
   k_invit<<<pl.nmol, kInvitThreads, sizeof(double) * 2 * (size_t)maxn, s>>>(pl, w);
 }
 
-void launch_backtransform(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s) {
-  dim3 grid((maxn + kBtCols - 1) / kBtCols, pl.nmol);
-  k_backtransform<<<grid, kBtCols * kBtGroups, sizeof(double) * (size_t)maxn, s>>>(pl, w);
+// 32 columns per block for the whole batch; 8 per block (4x the blocks per
+// molecule) for a short list of molecules.
+void launch_backtransform(const DevPlan &pl, const Work &w, int maxn, const int32_t *mol_list, int count,
+                          cudaStream_t s) {
+  if (count <= 0) return;
+  const size_t smem = sizeof(double) * (size_t)maxn;
+  if (mol_list) {
+    dim3 grid((maxn + 7) / 8, count);
+    k_backtransform<8><<<grid, kBtThreads, smem, s>>>(pl, w, mol_list);
+  } else {
+    dim3 grid((maxn + 31) / 32, count);
+    k_backtransform<32><<<grid, kBtThreads, smem, s>>>(pl, w, mol_list);
+  }
 }
+
 
 cudaError_t set_linalg_smem_limits(int maxn) {
   const size_t need = sizeof(double) * 2 * (size_t)maxn;

@@ -252,7 +252,10 @@ __global__ void __launch_bounds__(kMixThreads) k_charges_mix(DevParams p, DevPla
     if (!isfinite(l2)) flag = 3;
     else if (!lowp && iter > 0 && l2 < o.x_atol && mx < o.x_atol_max) flag = 1;
     else if (iter >= o.maxiter) flag = 2;
-    if (lowp && (flag == 2 || l2 < kLowpSwitch || iter + 1 >= kLowpMaxPasses)) w.prec[m] = 1;
+    if (lowp && (flag == 2 || l2 < kLowpSwitch || iter + 1 >= kLowpMaxPasses)) {
+      w.prec[m] = 1;
+      w.npass32[m] = iter + 1;
+    }
     s_flag = flag;
     if (flag == 3) {
       w.status[m] |= GBXTB_MOL_NONFINITE;

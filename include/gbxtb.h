@@ -164,6 +164,13 @@ GBXTB_API int gbxtb_singlepoint(gbxtb_plan *plan, const gbxtb_options *opts,
  * stream of that call. */
 GBXTB_API int gbxtb_get_status(gbxtb_plan *plan, int32_t *status, int32_t *iterations);
 
+/* Number of SCF passes per molecule that ran in FP32 in the last
+ * gbxtb_singlepoint (host array of nmol; 0 without mixed precision).  The
+ * molecule's remaining passes (gbxtb_get_status iterations + 1 in total)
+ * ran in FP64.  No counterpart in the reference (its SCF is FP64 or FP32
+ * throughout).  Synchronises the stream of that call. */
+GBXTB_API int gbxtb_get_fp32_passes(gbxtb_plan *plan, int32_t *passes);
+
 /* Per-class device time (ms) and kernel-launch counts of the last
  * gbxtb_singlepoint run with opts->profile = 1 (host arrays of
  * GBXTB_PROF_CLASSES); *total_launches receives all kernel launches of that

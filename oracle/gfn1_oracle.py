@@ -455,12 +455,15 @@ def reference_occupation(basis: Basis, chrg: float, spin):
     return n0, np.array([na, nb])
 
 
-def fermi_occupation(emo: np.ndarray, nab: np.ndarray, kt: float, maxiter: int = 200):
+def fermi_occupation(emo: np.ndarray, nab: np.ndarray, kt: float, maxiter: int = 200,
+                     thr: float | None = None):
     """Fermi-Dirac occupations per spin channel, Newton on E_F from the
     HOMO/LUMO midpoint until |sum f - n| <= sqrt(eps) in every channel
-    (wavefunction/filling.py:201-366)."""
+    (wavefunction/filling.py:201-366).  ``thr`` overrides the reference's
+    threshold sqrt(eps) (finite-difference checks use a tighter one: the
+    electron-count error of sqrt(eps) moves the energy by ~1e-8 Eh)."""
     nmo = emo.shape[0]
-    thr = math.sqrt(EPS)
+    thr = math.sqrt(EPS) if thr is None else thr
     res = 5.0 * 1e-15  # 5 * finfo(float64).resolution
     emos, efs, targets, nonempty = [], [], [], []
     for nel in nab:
@@ -592,7 +595,7 @@ def singlepoint(numbers, positions, chrg: float = 0.0, spin=None, forces: bool =
                 etemp: float = 300.0, maxiter: int = 300, x_atol: float = 1e-10,
                 x_atol_max: float = 1e-10, mixer: str = "anderson",
                 broyden_alpha: float = 0.3, broyden_memory: int = 20,
-                v_init: np.ndarray | None = None) -> Result:
+                v_init: np.ndarray | None = None, fermi_thr: float | None = None) -> Result:
     """GFN1 single point without dispersion (calculators/types/energy.py:78-402).
 
     ``mixer="anderson"`` replays the reference's single-system SCF loop
@@ -645,7 +648,7 @@ def singlepoint(numbers, positions, chrg: float = 0.0, spin=None, forces: bool =
         fp = linv @ f @ linv.T
         emo, u = np.linalg.eigh(0.5 * (fp + fp.T))
         c = linv.T @ u
-        occ = fermi_occupation(emo, nab, kt)
+        occ = fermi_occupation(emo, nab, kt, thr=fermi_thr)
         p = (c * occ.sum(0)) @ c.T
         q = n0 - np.einsum("ij,ji->i", p, smat)
         state.update(emo=emo, c=c, occ=occ, p=p, q=q)
