@@ -85,11 +85,11 @@ def test_synthetic_molecules_against_reference():
 
 
 def test_engine_replays_oracle_broyden():
-    """Same mixer on both sides: the GPU and the oracle follow the same SCF
-    trajectory (iteration counts) and agree to 1e-10 Eh."""
+    """Same mixer on both sides: the GPU (every pass in FP64) and the oracle
+    follow the same SCF trajectory (iteration counts) and agree to 1e-10 Eh."""
     mols = molgen.c3_forces(4)
     for num, pos in mols:
-        calc = calc_for(num)
+        calc = calc_for(num, mixed_precision=False)
         res = calc.singlepoint(torch.tensor(pos, device="cuda"), forces=True)
         r = go.singlepoint(num, pos, mixer="broyden")
         assert abs(res.energy.item() - r.energy) < 1e-10
