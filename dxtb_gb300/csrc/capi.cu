@@ -24,10 +24,11 @@ void launch_gemm(const DevPlan &pl, const Work &w, const int64_t *tile0, int64_t
                  int all, cudaStream_t s);
 void launch_tridiag(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s);
 void launch_lowp_copies(const DevPlan &pl, const Work &w, cudaStream_t s);
+void launch_tridiag_smem(const DevPlan &pl, const Work &w, cudaStream_t s);
 void launch_tridiag_cluster(const DevPlan &pl, const Work &w, const int32_t *mol_list, int count,
                             int maxn, cudaStream_t s);
 void launch_bisect(const DevPlan &pl, const Work &w, int maxn, double kt, const int32_t *mol_list, int count,
-                   int nsplit, cudaStream_t s);
+                   int threads, cudaStream_t s);
 void launch_invit(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s);
 void launch_backtransform(const DevPlan &pl, const Work &w, int maxn, const int32_t *mol_list, int count,
                           cudaStream_t s);
@@ -86,6 +87,7 @@ struct gbxtb_plan {
   bool has_run = false;
   int32_t *h_active = nullptr;  // pinned
   int num_sms = 0;
+  int smem_launches = 0;  // size classes with molecules (k_tridiag_smem launches per pass)
   // profiling
   cudaEvent_t ev[GBXTB_PROF_CLASSES][2] = {};
   bool ev_ready = false;
@@ -121,10 +123,11 @@ Layout make_layout(const DevPlan &pl) {
   L.add(d * pl.ngam);                                       // gam
   for (int k = 0; k < 4; ++k) L.add(d * pl.natom);          // cn erep qat dedcn
   L.add(d * 3 * pl.natom);                                  // grad
-  for (int k = 0; k < 7; ++k) L.add(i4 * pl.nmol);          // status phase iter kvec nhist prec npass32
+  for (int k = 0; k < 8; ++k) L.add(i4 * pl.nmol);          // status phase iter kvec nhist prec npass32 stall32
   L.add(d * 2 * pl.nmol);                                   // efermi
   L.add(d * 6 * pl.nmol);                                   // energy
   L.add(d * 2 * pl.nmol);                                   // resid
+  L.add(d * pl.nmol);                                       // best32
   L.add(i4 * 4);                                            // active
   L.add(i4 * pl.nmol);                                      // active_list
   return L;
@@ -148,7 +151,8 @@ Work make_work(const DevPlan &pl, void *base) {
   w.grad = D();
   w.status = I(); w.phase = I(); w.iter = I(); w.kvec = I(); w.nhist = I(); w.prec = I();
   w.npass32 = I();
-  w.efermi = D(); w.energy = D(); w.resid = D();
+  w.stall32 = I();
+  w.efermi = D(); w.energy = D(); w.resid = D(); w.best32 = D();
   w.active = I();
   w.active_list = I();
   return w;
@@ -307,6 +311,16 @@ int gbxtb_plan_create(gbxtb_ctx *ctx, int32_t nmol, const int32_t *numbers,
     md.nel[1] = nb;
   }
   tile0[nmol] = ntile;
+  // shared-memory size classes of the FP32 tridiagonalisation
+  std::vector<int32_t> bins[kSmemBins];
+  int bin_maxn[kSmemBins] = {};
+  for (int m = 0; m < nmol; ++m)
+    for (int c = 0; c < kSmemBins; ++c)
+      if (mol[m].nao <= kSmemBinN[c]) {
+        bins[c].push_back(m);
+        bin_maxn[c] = std::max(bin_maxn[c], mol[m].nao);
+        break;
+      }
   auto *pl = new (std::nothrow) gbxtb_plan();
   if (!pl) return fail(GBXTB_ERR_NOMEM, "host allocation failed");
   pl->ctx = ctx;
@@ -332,6 +346,8 @@ int gbxtb_plan_create(gbxtb_ctx *ctx, int32_t nmol, const int32_t *numbers,
   const size_t o_sm = L.add(4 * sh_atom.size());
   const size_t o_aos = L.add(4 * ao_sh.size());
   const size_t o_n0 = L.add(8 * ao_n0.size());
+  size_t o_bin[kSmemBins];
+  for (int c = 0; c < kSmemBins; ++c) o_bin[c] = L.add(4 * std::max<size_t>(1, bins[c].size()));
   cudaError_t e = cudaMalloc(&pl->dbuf, L.total);
   if (e != cudaSuccess) {
     delete pl;
@@ -353,6 +369,8 @@ int gbxtb_plan_create(gbxtb_ctx *ctx, int32_t nmol, const int32_t *numbers,
   up(o_sl, sh_l.data(), 4 * sh_atom.size());
   up(o_sm, sh_mol.data(), 4 * sh_atom.size());
   up(o_aos, ao_sh.data(), 4 * ao_sh.size());
+  for (int c = 0; c < kSmemBins; ++c)
+    if (!bins[c].empty()) up(o_bin[c], bins[c].data(), 4 * bins[c].size());
   e = up(o_n0, ao_n0.data(), 8 * ao_n0.size());
   if (e != cudaSuccess) {
     cudaFree(pl->dbuf);
@@ -372,6 +390,11 @@ int gbxtb_plan_create(gbxtb_ctx *ctx, int32_t nmol, const int32_t *numbers,
   d.sh_mol = (const int32_t *)(b + o_sm);
   d.ao_sh = (const int32_t *)(b + o_aos);
   d.ao_n0 = (const double *)(b + o_n0);
+  for (int c = 0; c < kSmemBins; ++c) {
+    d.bin_mols[c] = (const int32_t *)(b + o_bin[c]);
+    d.bin_count[c] = (int)bins[c].size();
+    d.bin_maxn[c] = bin_maxn[c];
+  }
   e = set_linalg_smem_limits(maxn);
   if (e != cudaSuccess) {
     cudaFree(pl->dbuf);
@@ -389,6 +412,7 @@ int gbxtb_plan_create(gbxtb_ctx *ctx, int32_t nmol, const int32_t *numbers,
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&pl->num_sms, cudaDevAttrMultiProcessorCount, dev);
   }
+  for (int c = 0; c < kSmemBins; ++c) pl->smem_launches += bins[c].empty() ? 0 : 1;
   pl->ws_bytes = make_layout(d).total;
   *workspace_bytes = pl->ws_bytes;
   *out = pl;
@@ -504,6 +528,8 @@ int gbxtb_singlepoint(gbxtb_plan *plan, const gbxtb_options *opts, const double 
   CK(cudaMemsetAsync(w.kvec, 0, sizeof(int32_t) * pl.nmol, s));
   CK(cudaMemsetAsync(w.nhist, 0, sizeof(int32_t) * pl.nmol, s));
   CK(cudaMemsetAsync(w.npass32, 0, sizeof(int32_t) * pl.nmol, s));
+  CK(cudaMemsetAsync(w.stall32, 0, sizeof(int32_t) * pl.nmol, s));
+  CK(cudaMemsetAsync(w.best32, 0x7f, sizeof(double) * pl.nmol, s));  // 1.4e306: no pass yet
   // 0: the first passes run in FP32; any non-zero byte pattern means FP64
   CK(cudaMemsetAsync(w.prec, opts->mixed_precision ? 0 : 1, sizeof(int32_t) * pl.nmol, s));
   CK(cudaMemsetAsync(w.vin, 0, sizeof(double) * pl.nsh, s));
@@ -536,17 +562,17 @@ int gbxtb_singlepoint(gbxtb_plan *plan, const gbxtb_options *opts, const double 
     // for bisection and back-transformation), working from the device-side
     // list of molecules still iterating
     const bool tail = it > 0 && active <= plan->num_sms;
+    if (opts->mixed_precision) launch_tridiag_smem(pl, w, s);
     if (tail)
       launch_tridiag_cluster(pl, w, w.active_list, active, plan->maxn, s);
     else
       launch_tridiag(pl, w, plan->maxn, s);
-    pf.end(GBXTB_PROF_TRIDIAG, 1);
+    pf.end(GBXTB_PROF_TRIDIAG, opts->mixed_precision ? 1 + plan->smem_launches : 1);
     pf.begin(GBXTB_PROF_BISECT);
     if (tail)
-      launch_bisect(pl, w, plan->maxn, opts->kt, w.active_list, active,
-                    std::max(4, (4 * plan->num_sms + active - 1) / active), s);
+      launch_bisect(pl, w, plan->maxn, opts->kt, w.active_list, active, 32, s);
     else
-      launch_bisect(pl, w, plan->maxn, opts->kt, nullptr, pl.nmol, 4, s);
+      launch_bisect(pl, w, plan->maxn, opts->kt, nullptr, pl.nmol, 256, s);
     pf.end(GBXTB_PROF_BISECT, 1);
     pf.begin(GBXTB_PROF_FERMI);
     launch_fermi(pl, w, opts->kt, opts->fermi_maxiter, s);

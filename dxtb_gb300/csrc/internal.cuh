@@ -19,6 +19,18 @@ namespace gbxtb {
 constexpr int kMaxPrim = GBXTB_MAX_PRIM;
 constexpr int kMaxL = 2;
 
+// FP32 passes tridiagonalise in shared memory (packed lower triangle, one
+// CTA per molecule).  On chip fit kSmemLocalMaxN AOs: (328 * 329 / 2 +
+// 2 * 400) floats = 219 KB of the 227 KB a CTA can have; molecules up to
+// kSmemTridiagMaxN AOs first run their leading steps in global memory.
+// Molecules are launched in size classes: n <= kSmemBinN[c] with
+// kSmemBinThreads[c] threads per CTA.
+constexpr int kSmemLocalMaxN = 328;
+constexpr int kSmemTridiagMaxN = 400;
+constexpr int kSmemBins = 3;
+constexpr int kSmemBinN[kSmemBins] = {96, 192, kSmemTridiagMaxN};
+constexpr int kSmemBinThreads[kSmemBins] = {256, 512, 1024};
+
 // molecule phases of the SCF state machine
 constexpr int kPhaseIterate = 0;  // mixing iterations
 constexpr int kPhaseFinal = 1;    // one more V -> Q pass with the unmixed potential
@@ -55,6 +67,9 @@ struct DevPlan {
   const int32_t *sh_atom, *sh_rec, *sh_ao, *sh_l, *sh_mol;  // sh_ao: AO offset inside the molecule
   const int32_t *ao_sh;                                       // global shell of each AO
   const double *ao_n0;                                        // reference occupation per AO
+  const int32_t *bin_mols[kSmemBins];  // molecules of each shared-memory size class
+  int bin_count[kSmemBins];
+  int bin_maxn[kSmemBins];             // largest molecule of each class
 };
 
 // Device scratch of one singlepoint call.
@@ -79,6 +94,8 @@ struct Work {
   int32_t *status, *phase, *iter, *kvec, *nhist;
   int32_t *prec;    // 0: the next pass runs in FP32, 1: in FP64
   int32_t *npass32; // number of FP32 passes the molecule made
+  int32_t *stall32; // FP32 passes since the potential change last halved
+  double *best32;   // smallest potential change of the FP32 passes
   double *efermi;   // [2][nmol]
   double *energy;   // [nmol][6]: total, rep, h0, es2, es3, fermi
   double *resid;    // [nmol][2]: L2, max norm of the last potential change

@@ -38,6 +38,7 @@
 
 #include <cmath>
 #include <cooperative_groups.h>
+#include <mutex>
 
 namespace cg = cooperative_groups;
 
@@ -58,7 +59,10 @@ template <> struct Num<double> {
 template <> struct Num<float> {
   static constexpr double eps = 1.1920928955078125e-07;
   static constexpr double safemin = 1.1754943508222875e-38;
-  static constexpr double ctol = 1e-3;
+  // a wider FP32 window chains whole valence bands into one cluster (the
+  // MGS cost grows with its square); vectors of FP32 passes may be
+  // non-orthogonal to ~1e-3, which the SCF tolerates until the FP64 passes
+  static constexpr double ctol = 1e-4;
 };
 
 // FP32 or FP64 view of a per-molecule n x n work block.
@@ -436,12 +440,194 @@ __global__ void __launch_bounds__(kTrdThreads) k_tridiag(DevPlan pl, Work w) {
   const int m = blockIdx.x;
   if (w.phase[m] == kPhaseDone) return;
   const MolDesc md = pl.mol[m];
+  if (w.prec[m] == 0 && md.nao <= kSmemTridiagMaxN) return;  // k_tridiag_smem
   extern __shared__ double sm[];
   __shared__ double red[32];
   if (w.prec[m])
     tridiag_body<double>(md, w, sm, red);
   else
     tridiag_body<float>(md, w, reinterpret_cast<float *>(sm), reinterpret_cast<float *>(red));
+}
+
+// ---------------------------------------------------------------------------
+// FP32 Householder tridiagonalisation with the matrix in shared memory
+// (packed lower triangle, row i at i(i+1)/2), one CTA per molecule.  Every
+// operand of a step is an on-chip access and a step needs five CTA
+// barriers, instead of the L2 round trips and cluster barriers of the
+// global-memory kernels; this is the kernel of the FP32 passes (most passes
+// of every molecule, all passes of molecules that do not converge).
+// A molecule with more than kSmemLocalMaxN AOs first runs its leading
+// n - kSmemLocalMaxN steps on the FP32 view of A in global memory (same
+// steps as tridiag_body<float>), then loads the trailing matrix on chip.
+// Output conventions as tridiag_body<float>: reflector k in row k of the
+// FP32 view of A (for the back-transformation), d, e, tau in FP64 arrays.
+// Launched per size class (kSmemBins) over the plan's per-class molecule
+// lists; molecules of an FP64 pass or already done return at once.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int64_t poff(int i) { return (int64_t)i * (i + 1) / 2; }
+
+// Sum over the CTA with one barrier: warp partials go to red[0..nw-1] and
+// every thread adds them up.  Consecutive calls must alternate between two
+// `red` buffers (the next write to a buffer comes after another barrier).
+__device__ __forceinline__ float cta_sum(float v, float *red) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  v = warp_sum(v);
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  float t = 0.f;
+  for (int i = 0; i < nw; ++i) t += red[i];
+  return t;
+}
+
+__global__ void __launch_bounds__(1024) k_tridiag_smem(DevPlan pl, Work w, const int32_t *mol_list) {
+  const int m = mol_list[blockIdx.x];
+  if (w.phase[m] == kPhaseDone || w.prec[m] != 0) return;
+  const MolDesc md = pl.mol[m];
+  const int n = md.nao;
+  const int k0 = n > kSmemLocalMaxN ? n - kSmemLocalMaxN : 0;  // steps in global memory
+  const int nl = n - k0;                                        // trailing size on chip
+  extern __shared__ float smf[];
+  float *Ap = smf;                     // packed lower triangle of A[k0.., k0..]
+  float *vs = smf + poff(nl);          // [n]
+  float *ps = vs + n;                  // [n]
+  __shared__ float red[4][32];
+  float *Ag = mat_view<float>(w.A, md.mat0);
+  double *d = w.d + md.ao0, *e = w.e + md.ao0, *tau = w.tau + md.ao0;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int rb = 0;  // alternating reduction buffer
+
+  // leading steps on the full matrix in global memory
+  for (int k = 0; k < k0; ++k) {
+    const int m1 = n - k - 1;
+    float part = 0.f;
+    for (int t = 1 + threadIdx.x; t < m1; t += blockDim.x) {
+      const float x = Ag[(int64_t)(k + 1 + t) * n + k];
+      part += x * x;
+    }
+    const float xn2 = cta_sum(part, red[rb]);
+    rb ^= 1;
+    const float alpha = Ag[(int64_t)(k + 1) * n + k];
+    float tk = 0.f, scale = 0.f, beta = alpha;
+    if (xn2 != 0.f) {
+      beta = -copysignf(sqrtf(alpha * alpha + xn2), alpha);
+      tk = (beta - alpha) / beta;
+      scale = 1.f / (alpha - beta);
+    }
+    if (threadIdx.x == 0) {
+      d[k] = Ag[(int64_t)k * n + k];
+      e[k] = beta;
+      tau[k] = tk;
+    }
+    if (tk == 0.f) continue;  // uniform; nothing was written
+    for (int t = threadIdx.x; t < m1; t += blockDim.x)
+      vs[t] = (t == 0) ? 1.f : Ag[(int64_t)(k + 1 + t) * n + k] * scale;
+    __syncthreads();
+    for (int t = threadIdx.x; t < m1; t += blockDim.x) Ag[(int64_t)k * n + k + 1 + t] = vs[t];
+    float pv = 0.f;
+    for (int i = wid; i < m1; i += nw) {
+      const float *row = Ag + (int64_t)(k + 1 + i) * n + (k + 1);
+      float sacc = 0.f;
+      for (int j = lane; j < m1; j += 32) sacc += row[j] * vs[j];
+      sacc = warp_sum(sacc) * tk;
+      if (lane == 0) {
+        ps[i] = sacc;
+        pv += sacc * vs[i];
+      }
+    }
+    const float K = cta_sum(pv, red[rb]);
+    rb ^= 1;
+    const float half = 0.5f * tk * K;
+    for (int i = wid; i < m1; i += nw) {
+      float *row = Ag + (int64_t)(k + 1 + i) * n + (k + 1);
+      const float vi = vs[i], wi = ps[i] - half * vs[i];
+      for (int j = lane; j < m1; j += 32) row[j] -= vi * (ps[j] - half * vs[j]) + wi * vs[j];
+    }
+    __syncthreads();
+  }
+
+  // the trailing matrix on chip (lower triangle, local indices)
+  for (int i = wid; i < nl; i += nw)
+    for (int j = lane; j <= i; j += 32) Ap[poff(i) + j] = Ag[(int64_t)(k0 + i) * n + k0 + j];
+  __syncthreads();
+  for (int kl = 0; kl + 2 < nl; ++kl) {
+    const int k = k0 + kl;   // global step
+    const int m1 = nl - kl - 1;
+    float part = 0.f;
+    for (int t = 1 + threadIdx.x; t < m1; t += blockDim.x) {
+      const float x = Ap[poff(kl + 1 + t) + kl];
+      part += x * x;
+    }
+    const float xn2 = cta_sum(part, red[rb]);
+    rb ^= 1;
+    // every thread derives the reflector parameters (identical values)
+    const float alpha = Ap[poff(kl + 1) + kl];
+    float tk = 0.f, scale = 0.f, beta = alpha;
+    if (xn2 != 0.f) {
+      beta = -copysignf(sqrtf(alpha * alpha + xn2), alpha);
+      tk = (beta - alpha) / beta;
+      scale = 1.f / (alpha - beta);
+    }
+    if (threadIdx.x == 0) {
+      d[k] = Ap[poff(kl) + kl];
+      e[k] = beta;
+      tau[k] = tk;
+    }
+    if (tk == 0.f) continue;  // uniform; nothing was written
+    for (int t = threadIdx.x; t < m1; t += blockDim.x) {
+      const float v = (t == 0) ? 1.f : Ap[poff(kl + 1 + t) + kl] * scale;
+      vs[t] = v;
+      Ag[(int64_t)k * n + k + 1 + t] = v;  // reflector for the back-transformation
+    }
+    __syncthreads();
+    // p = tau A22 v: lower part by rows (two rows per warp in flight) ...
+    for (int t = wid; t < m1; t += 2 * nw) {
+      const int t2 = t + nw;
+      const float *r1 = Ap + poff(kl + 1 + t) + (kl + 1);
+      const float *r2 = Ap + poff(kl + 1 + min(t2, m1 - 1)) + (kl + 1);
+      float s1 = 0.f, s2 = 0.f;
+      for (int j = lane; j <= t; j += 32) s1 += r1[j] * vs[j];
+      if (t2 < m1)
+        for (int j = lane; j <= t2; j += 32) s2 += r2[j] * vs[j];
+      s1 = warp_sum(s1);
+      s2 = warp_sum(s2);
+      if (lane == 0) {
+        ps[t] = s1;
+        if (t2 < m1) ps[t2] = s2;
+      }
+    }
+    __syncthreads();
+    // ... strict upper part by columns, then K = p.v
+    float pv = 0.f;
+    for (int j = wid; j < m1; j += nw) {
+      float sacc = 0.f;
+      for (int i = j + 1 + lane; i < m1; i += 32) sacc += Ap[poff(kl + 1 + i) + kl + 1 + j] * vs[i];
+      sacc = warp_sum(sacc);
+      if (lane == 0) {
+        const float pj = tk * (ps[j] + sacc);
+        ps[j] = pj;
+        pv += pj * vs[j];
+      }
+    }
+    const float K = cta_sum(pv, red[rb]);
+    rb ^= 1;
+    const float half = 0.5f * tk * K;
+    // A22 -= v w^T + w v^T (lower triangle), w = p - half v
+    for (int t = wid; t < m1; t += nw) {
+      float *row = Ap + poff(kl + 1 + t) + (kl + 1);
+      const float vi = vs[t], wi = ps[t] - half * vs[t];
+      for (int j = lane; j <= t; j += 32) row[j] -= vi * (ps[j] - half * vs[j]) + wi * vs[j];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    if (nl >= 2) {
+      d[n - 2] = Ap[poff(nl - 2) + nl - 2];
+      d[n - 1] = Ap[poff(nl - 1) + nl - 1];
+      e[n - 2] = Ap[poff(nl - 1) + nl - 2];
+    } else {
+      d[n - 1] = Ap[0];
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -562,7 +748,9 @@ __global__ void __cluster_dims__(kClusterSize, 1, 1) __launch_bounds__(kTrdClThr
   extern __shared__ double sm[];
   __shared__ double red[32];
   __shared__ double kpart;
-  const bool done = (w.phase[m] == kPhaseDone);  // uniform over the cluster
+  // uniform over the cluster; FP32 passes of molecules that fit in shared
+  // memory run in k_tridiag_smem
+  const bool done = (w.phase[m] == kPhaseDone) || (w.prec[m] == 0 && md.nao <= kSmemTridiagMaxN);
   if (!done) {
     if (w.prec[m])
       tridiag_cluster_body<double>(cluster, md, w, sm, red, &kpart);
@@ -652,72 +840,136 @@ __device__ __forceinline__ int sturm_count(const float *ds, const float *e2, int
 }
 
 
+// Newton correction -p_n(x) / p_n'(x) of the characteristic polynomial
+// p_n(x) = det(T - x I) of the tridiagonal (ds, e2 = e^2):
+//   p_{j+1} = (d_j - x) p_j - e_{j-1}^2 p_{j-1},
+//   p'_{j+1} = (d_j - x) p'_j - p_j - e_{j-1}^2 p'_{j-1},
+// all four running values rescaled together by powers of two.
+__device__ __forceinline__ double newton_correction(const double *ds, const double *e2, int n, double x) {
+  double pm = 1.0, pc = ds[0] - x;  // p_{j-1}, p_j
+  double qm = 0.0, qc = -1.0;       // p'_{j-1}, p'_j
+  for (int j = 1; j < n; ++j) {
+    const double a = ds[j] - x, b = e2[j - 1];
+    const double pn = fma(a, pc, -b * pm);
+    const double qn = fma(a, qc, -fma(b, qm, pc));
+    pm = pc;
+    pc = pn;
+    qm = qc;
+    qc = qn;
+    const double mag = fmax(fmax(fabs(pc), fabs(qc)), fmax(fabs(pm), fabs(qm)));
+    const int ex = (int)((__double_as_longlong(mag) >> 52) & 0x7ff);
+    if (ex > 1023 + 400) {
+      pm *= 0x1p-400; pc *= 0x1p-400; qm *= 0x1p-400; qc *= 0x1p-400;
+    } else if (ex < 1023 - 400 && mag != 0.0) {
+      pm *= 0x1p+400; pc *= 0x1p+400; qm *= 0x1p+400; qc *= 0x1p+400;
+    }
+  }
+  return (qc != 0.0 && isfinite(pc) && isfinite(qc)) ? -pc / qc : 0.0;
+}
+
+// Eigenvalues of one molecule's tridiagonal matrix.
+//
+// Only eigenvalues that can carry occupation are computed: those below the
+// cut = (LUMO bracket) + 60 kT + 0.01 Eh.  Above it (E - E_F)/kT >= 50, where
+// the occupation is exactly zero, so those eigenvalues only enter the Fermi
+// iteration through their count; they get placeholder values above the cut
+// (ascending), which gives the same occupations.
+//
+// FP32 pass: bisection of the FP32 copy of the matrix to FP32 resolution.
+// FP64 pass: the same FP32 bisection as the start value, then Newton on the
+// FP64 characteristic polynomial (quadratic convergence from ~1e-7), then a
+// check with two FP64 Sturm counts that the result is the eigenvalue of this
+// index; on failure (a near-degenerate cluster) full FP64 bisection.  This
+// needs ~8 FP64 count-equivalents per eigenvalue instead of ~55.
+// (Every loop is bounded: a non-finite matrix ends with a garbage value,
+// which the SCF status check turns into an error, never in a hang.)
 template <typename T>
 __device__ __forceinline__ void bisect_body(const MolDesc &md, const Work &w, int part, int nsplit,
-                                            double kt, T *sm, double *red) {
+                                            double kt, double *sm, double *red) {
   const int n = md.nao;
-  T *ds = sm, *e2 = sm + n;
+  double *ds = sm, *e2 = sm + n;                                  // FP64 pass only
+  float *ds32 = reinterpret_cast<float *>(sm + 2 * n), *e2_32 = ds32 + n;
   __shared__ double s_cut;
+  __shared__ int s_ncut;
   const double *d = w.d + md.ao0, *e = w.e + md.ao0;
   double *ev = w.eig + md.ao0;
+  constexpr bool kFp64 = sizeof(T) == 8;
   double glo = 1e300, ghi = -1e300, emax = 0.0;
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    ds[i] = (T)d[i];
+    const double ee = (i < n - 1) ? e[i] * e[i] : 0.0;
+    if (kFp64) {
+      ds[i] = d[i];
+      e2[i] = ee;
+    }
+    ds32[i] = (float)d[i];
+    e2_32[i] = (float)ee;
     const double el = (i > 0) ? fabs(e[i - 1]) : 0.0;
     const double er = (i < n - 1) ? fabs(e[i]) : 0.0;
-    e2[i] = (i < n - 1) ? (T)(e[i] * e[i]) : T(0);
     glo = fmin(glo, d[i] - el - er);
     ghi = fmax(ghi, d[i] + el + er);
-    emax = fmax(emax, (i < n - 1) ? e[i] * e[i] : 0.0);
+    emax = fmax(emax, ee);
   }
   glo = block_min(glo, red);
   ghi = block_max(ghi, red);
   emax = block_max(emax, red);
   const double tnorm = fmax(fabs(glo), fabs(ghi));
-  glo -= 2.0 * Num<T>::eps * tnorm * n + 1e-300;
-  ghi += 2.0 * Num<T>::eps * tnorm * n + 1e-300;
-  const T pivmin = (T)(Num<T>::safemin * fmax(1.0, emax));
+  // the FP32 copy differs from the matrix by <= eps32 |T| per entry
+  const double glo32 = glo - 4.0 * Num<float>::eps * tnorm * n - 1e-30;
+  const double ghi32 = ghi + 4.0 * Num<float>::eps * tnorm * n + 1e-30;
+  const float piv32 = (float)(Num<float>::safemin * fmax(1.0, emax));
+  const double piv64 = Num<double>::safemin * fmax(1.0, emax);
   // index of the lowest eigenvalue of the alpha channel that is empty at T=0
   const int lumo = min(n - 1, (int)ceil(md.nel[0] - 5.0e-15));
-  // pass 1: every eigenvalue of this part to 1e-4, plus (thread 0) the LUMO
-  // bracket that fixes the refinement window
-  // (every loop is bounded: a non-finite matrix ends with a garbage value,
-  //  which the SCF status check turns into an error, never in a hang)
-  const int stride = blockDim.x * nsplit;
   if (threadIdx.x == 0) {
-    T lo = (T)glo, hi = (T)ghi;
-    for (int it = 0; it < 96 && hi - lo > T(1.0e-4); ++it) {
-      const T mid = T(0.5) * (lo + hi);
-      if (sturm_count(ds, e2, n, mid, pivmin) <= lumo) lo = mid; else hi = mid;
+    float lo = (float)glo32, hi = (float)ghi32;
+    for (int it = 0; it < 96 && hi - lo > 1.0e-4f; ++it) {
+      const float mid = 0.5f * (lo + hi);
+      if (sturm_count(ds32, e2_32, n, mid, piv32) <= lumo) lo = mid; else hi = mid;
     }
-    s_cut = (double)hi + 60.0 * kt + 0.01;
-  }
-  for (int idx = part * blockDim.x + threadIdx.x; idx < n; idx += stride) {
-    T lo = (T)glo, hi = (T)ghi;
-    for (int it = 0; it < 96 && hi - lo > T(1.0e-4); ++it) {
-      const T mid = T(0.5) * (lo + hi);
-      if (sturm_count(ds, e2, n, mid, pivmin) <= idx) lo = mid; else hi = mid;
-    }
-    ev[idx] = (double)lo;            // lower bracket
+    const double cut = (double)hi + 60.0 * kt + 0.01;
+    s_cut = cut;
+    s_ncut = max(lumo + 1, min(n, sturm_count(ds32, e2_32, n, (float)cut, piv32)));
   }
   __syncthreads();
   const double cut = s_cut;
-  // pass 2: full precision below the cut
+  const int ncut = s_ncut;
+  const int stride = blockDim.x * nsplit;
   for (int idx = part * blockDim.x + threadIdx.x; idx < n; idx += stride) {
-    T lo = (T)ev[idx];
-    T hi = lo + T(1.0e-4);
-    if ((double)lo < cut) {
-      hi = fmin(hi + T(1.0e-4), (T)ghi);
-      // re-establish a valid upper bracket
-      for (int it = 0; it < 64 && sturm_count(ds, e2, n, hi, pivmin) <= idx; ++it)
-        hi = fmin(hi + T(1.0e-3), (T)(ghi + 1.0));
-      for (int it = 0; it < 128; ++it) {
-        const T mid = T(0.5) * (lo + hi);
-        if (mid <= lo || mid >= hi) break;
-        if (sturm_count(ds, e2, n, mid, pivmin) <= idx) lo = mid; else hi = mid;
+    if (idx >= ncut) {
+      ev[idx] = cut + 1.0 + 1.0e-3 * (idx - ncut);  // empty orbital (placeholder)
+      continue;
+    }
+    // FP32 bisection to the resolution of the FP32 copy (eps32 |T|)
+    const float ftol = (float)(2.0 * Num<float>::eps * tnorm);
+    float lo = (float)glo32, hi = (float)fmax(cut, ghi32);
+    for (int it = 0; it < 96 && hi - lo > ftol; ++it) {
+      const float mid = 0.5f * (lo + hi);
+      if (mid <= lo || mid >= hi) break;
+      if (sturm_count(ds32, e2_32, n, mid, piv32) <= idx) lo = mid; else hi = mid;
+    }
+    double x = 0.5 * ((double)lo + (double)hi);
+    if (kFp64) {
+      const double tol = 4.0 * Num<double>::eps * tnorm;
+      for (int it = 0; it < 6; ++it) {
+        const double dx = newton_correction(ds, e2, n, x);
+        x += dx;
+        if (!(fabs(dx) > tol)) break;
+      }
+      const double delta = 64.0 * Num<double>::eps * tnorm + 1e-300;
+      const bool ok = isfinite(x) && sturm_count(ds, e2, n, x - delta, piv64) <= idx &&
+                      sturm_count(ds, e2, n, x + delta, piv64) > idx;
+      if (!ok) {
+        double blo = glo - 2.0 * Num<double>::eps * tnorm * n - 1e-300;
+        double bhi = fmax(cut, ghi) + 2.0 * Num<double>::eps * tnorm * n + 1e-300;
+        for (int it = 0; it < 128; ++it) {
+          const double mid = 0.5 * (blo + bhi);
+          if (mid <= blo || mid >= bhi) break;
+          if (sturm_count(ds, e2, n, mid, piv64) <= idx) blo = mid; else bhi = mid;
+        }
+        x = 0.5 * (blo + bhi);
       }
     }
-    ev[idx] = 0.5 * ((double)lo + (double)hi);
+    ev[idx] = x;
   }
 }
 
@@ -735,8 +987,9 @@ __global__ void __launch_bounds__(256) k_bisect(DevPlan pl, Work w, double kt, c
   if (w.prec[m])
     bisect_body<double>(md, w, part, gridDim.y, kt, sm, red);
   else
-    bisect_body<float>(md, w, part, gridDim.y, kt, reinterpret_cast<float *>(sm), red);
+    bisect_body<float>(md, w, part, gridDim.y, kt, sm, red);
 }
+
 
 
 // ---------------------------------------------------------------------------
@@ -795,17 +1048,22 @@ __device__ __forceinline__ void invit_factor(int n, int i, T lam, const T *d, co
 template <typename T>
 __device__ __forceinline__ void invit_solve(int n, int i, const T *U1, const T *U2, const T *U3, const T *LM,
                                             const T *PV, T *Y) {
+  // forward sweep with the running component in a register (no store->load
+  // dependence through memory from one step to the next)
+  T carry = Y[i];
   for (int j = 0; j < n - 1; ++j) {
     const int64_t o = (int64_t)j * n + i;
-    const T yj = Y[o], yj1 = Y[o + n];
+    const T yj1 = Y[o + n];
     const T l = LM[o];
     if (PV[o] != T(0)) {
       Y[o] = yj1;
-      Y[o + n] = yj - l * yj1;
+      carry = carry - l * yj1;
     } else {
-      Y[o + n] = yj1 - l * yj;
+      Y[o] = carry;
+      carry = yj1 - l * carry;
     }
   }
+  Y[(int64_t)(n - 1) * n + i] = carry;
   T x1 = T(0), x2 = T(0), nrm = T(0);
   for (int j = n - 1; j >= 0; --j) {
     const int64_t o = (int64_t)j * n + i;
@@ -818,13 +1076,14 @@ __device__ __forceinline__ void invit_solve(int n, int i, const T *U1, const T *
   const T inv = (nrm > T(0)) ? T(1) / nrm : T(1);
   T s2 = T(0);
   for (int j = 0; j < n; ++j) {
-    const int64_t o = (int64_t)j * n + i;
-    const T y = Y[o] * inv;
-    Y[o] = y;
+    const T y = Y[(int64_t)j * n + i] * inv;
     s2 += y * y;
   }
   const T in2 = T(1) / sqrt(s2);
-  for (int j = 0; j < n; ++j) Y[(int64_t)j * n + i] *= in2;
+  for (int j = 0; j < n; ++j) {
+    const int64_t o = (int64_t)j * n + i;
+    Y[o] = (Y[o] * inv) * in2;
+  }
 }
 
 // Modified Gram-Schmidt inside every cluster of close eigenvalues, one warp
@@ -882,7 +1141,7 @@ __device__ __forceinline__ void invit_body(const MolDesc &md, const Work &w, T *
   const double tnorm = block_max(tl, red);
   // eigenvalues closer than ctol |T| are orthogonalised explicitly; others
   // come out orthogonal to eps |T| / gap from inverse iteration
-  // (FP64: <= 2e-12; FP32: <= 1e-4, enough for the early SCF passes)
+  // (FP64: <= 2e-12; FP32: <= 1e-3, enough for the early SCF passes)
   const double ctol = Num<T>::ctol * tnorm;
   const T pert = (T)(Num<T>::eps * tnorm);
   for (int i = threadIdx.x; i < kvec; i += blockDim.x) {
@@ -976,6 +1235,62 @@ __global__ void __launch_bounds__(kBtThreads) k_backtransform(DevPlan pl, Work w
                                     reinterpret_cast<float *>(part), reinterpret_cast<float *>(sfac));
 }
 
+// Back-transformation with one warp per eigenvector: the column lives in
+// registers (row r in lane r % 32, slot r / 32), so applying a reflector is a
+// warp reduction and a register update, with no CTA barrier; the reflector
+// rows are read through L1, shared by the eight warps of a CTA.
+template <typename T, int NQ>
+__device__ __forceinline__ void backtransform_column(const MolDesc &md, const Work &w, int c) {
+  const int n = md.nao;
+  const int lane = threadIdx.x & 31;
+  const T *A = mat_view<T>(w.A, md.mat0);
+  const double *tau = w.tau + md.ao0;
+  T *Y = mat_view<T>(w.Z, md.mat0);
+  T y[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    const int r = lane + 32 * q;
+    y[q] = (r < n) ? Y[(int64_t)r * n + c] : T(0);
+  }
+  for (int k = n - 3; k >= 0; --k) {
+    const T tk = (T)tau[k];
+    if (tk == T(0)) continue;
+    const T *v = A + (int64_t)k * n;  // reflector k: v[r] = A[k][r] multiplies row r > k
+    T vq[NQ];
+    T dot = T(0);
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      const int r = lane + 32 * q;
+      vq[q] = (r > k && r < n) ? v[r] : T(0);
+      dot += vq[q] * y[q];
+    }
+    dot = warp_sum(dot) * tk;
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) y[q] -= dot * vq[q];
+  }
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    const int r = lane + 32 * q;
+    if (r < n) Y[(int64_t)r * n + c] = y[q];
+  }
+}
+
+// grid (column groups of 8, molecules): molecule mol_list[y] (all if null);
+// every molecule has at most 32 * NQ AOs
+template <int NQ>
+__global__ void __launch_bounds__(256) k_backtransform_warp(DevPlan pl, Work w, const int32_t *mol_list) {
+  const int m = mol_list ? mol_list[blockIdx.y] : (int)blockIdx.y;
+  if (w.phase[m] == kPhaseDone) return;
+  const MolDesc md = pl.mol[m];
+  const int kvec = min(max(w.kvec[m], 0), md.nao);
+  const int c = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (c >= kvec) return;  // whole warp
+  if (w.prec[m])
+    backtransform_column<double, NQ>(md, w, c);
+  else
+    backtransform_column<float, NQ>(md, w, c);
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -999,6 +1314,18 @@ void launch_tridiag(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s) 
   k_tridiag<<<pl.nmol, kTrdThreads, smem, s>>>(pl, w);
 }
 
+// FP32 passes of molecules with at most kSmemTridiagMaxN AOs, one launch
+// per size class.
+void launch_tridiag_smem(const DevPlan &pl, const Work &w, cudaStream_t s) {
+  for (int c = 0; c < kSmemBins; ++c) {
+    if (pl.bin_count[c] <= 0) continue;
+    const int nmax = pl.bin_maxn[c];
+    const int nloc = nmax < kSmemLocalMaxN ? nmax : kSmemLocalMaxN;
+    const size_t smem = sizeof(float) * ((size_t)nloc * (nloc + 1) / 2 + 2 * (size_t)nmax);
+    k_tridiag_smem<<<pl.bin_count[c], kSmemBinThreads[c], smem, s>>>(pl, w, pl.bin_mols[c]);
+  }
+}
+
 // Cluster tridiagonalisation for the molecules listed in mol_list (device).
 void launch_tridiag_cluster(const DevPlan &pl, const Work &w, const int32_t *mol_list, int count,
                             int maxn, cudaStream_t s) {
@@ -1007,27 +1334,39 @@ void launch_tridiag_cluster(const DevPlan &pl, const Work &w, const int32_t *mol
   k_tridiag_cluster<<<count * kClusterSize, kTrdClThreads, smem, s>>>(pl, w, mol_list);
 }
 
-// All molecules (mol_list null, count = nmol) or the listed ones; nsplit
-// blocks per molecule.
+// All molecules (mol_list null, count = nmol) with 256 threads per block,
+// or the listed ones with `threads` per block and as many blocks as the
+// largest molecule needs (more SMs per molecule for a short list).
 void launch_bisect(const DevPlan &pl, const Work &w, int maxn, double kt, const int32_t *mol_list, int count,
-                   int nsplit, cudaStream_t s) {
+                   int threads, cudaStream_t s) {
   if (count <= 0) return;
-  const size_t smem = sizeof(double) * 2 * (size_t)maxn;
-  const int maxsplit = (maxn + 255) / 256;
-  dim3 grid(count, max(1, min(nsplit, maxsplit)));
-  k_bisect<<<grid, 256, smem, s>>>(pl, w, kt, mol_list);
+  const size_t smem = sizeof(double) * 3 * (size_t)maxn;
+  dim3 grid(count, (maxn + threads - 1) / threads);
+  k_bisect<<<grid, threads, smem, s>>>(pl, w, kt, mol_list);
 }
+
 
 
 void launch_invit(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s) {
   k_invit<<<pl.nmol, kInvitThreads, sizeof(double) * 2 * (size_t)maxn, s>>>(pl, w);
 }
 
-// 32 columns per block for the whole batch; 8 per block (4x the blocks per
-// molecule) for a short list of molecules.
+// Warp-per-eigenvector kernel up to 384 AOs; beyond that 32 columns per
+// block for the whole batch and 8 per block (4x the blocks per molecule) for
+// a short list of molecules.
 void launch_backtransform(const DevPlan &pl, const Work &w, int maxn, const int32_t *mol_list, int count,
                           cudaStream_t s) {
   if (count <= 0) return;
+  if (maxn <= 384) {
+    dim3 grid((maxn + 7) / 8, count);
+    if (maxn <= 128)
+      k_backtransform_warp<4><<<grid, 256, 0, s>>>(pl, w, mol_list);
+    else if (maxn <= 256)
+      k_backtransform_warp<8><<<grid, 256, 0, s>>>(pl, w, mol_list);
+    else
+      k_backtransform_warp<12><<<grid, 256, 0, s>>>(pl, w, mol_list);
+    return;
+  }
   const size_t smem = sizeof(double) * (size_t)maxn;
   if (mol_list) {
     dim3 grid((maxn + 7) / 8, count);
@@ -1039,21 +1378,38 @@ void launch_backtransform(const DevPlan &pl, const Work &w, int maxn, const int3
 }
 
 
+
+// Dynamic shared-memory limits of the kernels whose footprint grows with the
+// largest molecule of a plan.  The attribute is per function and process
+// wide, and plans created earlier keep launching, so it only ever grows.
 cudaError_t set_linalg_smem_limits(int maxn) {
-  const size_t need = sizeof(double) * 2 * (size_t)maxn;
-  cudaError_t e = cudaSuccess;
-  if (need > 48 * 1024) {
-    e = cudaFuncSetAttribute(k_tridiag, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_bisect, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_invit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need);
-    if (e != cudaSuccess) return e;
-  }
+  static std::mutex mu;
+  static size_t cur_smem = 0, cur2 = 0, cur3 = 0;
+  std::lock_guard<std::mutex> lock(mu);
+  const int nb = maxn < kSmemLocalMaxN ? maxn : kSmemLocalMaxN;
+  const int nv = maxn < kSmemTridiagMaxN ? maxn : kSmemTridiagMaxN;
+  const size_t need_s = sizeof(float) * ((size_t)nb * (nb + 1) / 2 + 2 * (size_t)nv);
+  const size_t need2 = sizeof(double) * 2 * (size_t)maxn;
   const size_t need3 = sizeof(double) * 3 * (size_t)maxn;
-  if (need3 > 48 * 1024) {
+  cudaError_t e = cudaSuccess;
+  if (need_s > 48 * 1024 && need_s > cur_smem) {
+    e = cudaFuncSetAttribute(k_tridiag_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need_s);
+    if (e != cudaSuccess) return e;
+    cur_smem = need_s;
+  }
+  if (need2 > 48 * 1024 && need2 > cur2) {
+    e = cudaFuncSetAttribute(k_tridiag, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need2);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_invit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need2);
+    if (e != cudaSuccess) return e;
+    cur2 = need2;
+  }
+  if (need3 > 48 * 1024 && need3 > cur3) {
+    e = cudaFuncSetAttribute(k_bisect, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need3);
+    if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(k_tridiag_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need3);
     if (e != cudaSuccess) return e;
+    cur3 = need3;
   }
   return e;
 }

@@ -122,9 +122,17 @@ __device__ __forceinline__ double wdot(const double *a, const double *b, const i
 
 constexpr int kMixThreads = 256;
 // mixed precision: potential change (orbital L2 norm) below which a molecule
-// leaves the FP32 passes, and the most FP32 passes a molecule makes
+// leaves the FP32 passes (FP32 noise in the potential is ~1e-6), and a cap on
+// the FP32 passes far beyond the iteration counts seen (molecules that never
+// converge keep iterating in FP32 until maxiter; their final pass is FP64)
 constexpr double kLowpSwitch = 1e-4;
-constexpr int kLowpMaxPasses = 40;
+constexpr int kLowpMaxPasses = 1000;
+// a molecule whose FP32 passes stop making progress close to convergence
+// (potential change below kLowpStallBelow and not halved for kLowpStall
+// passes: the FP32 noise floor) continues in FP64; molecules that do not
+// converge at all oscillate far above it and stay in FP32
+constexpr double kLowpStallBelow = 1e-3;
+constexpr int kLowpStall = 8;
 constexpr int kMaxMem = 30;
 
 __global__ void __launch_bounds__(kMixThreads) k_charges_mix(DevParams p, DevPlan pl, Work w, MixOpts o) {
@@ -252,7 +260,17 @@ __global__ void __launch_bounds__(kMixThreads) k_charges_mix(DevParams p, DevPla
     if (!isfinite(l2)) flag = 3;
     else if (!lowp && iter > 0 && l2 < o.x_atol && mx < o.x_atol_max) flag = 1;
     else if (iter >= o.maxiter) flag = 2;
-    if (lowp && (flag == 2 || l2 < kLowpSwitch || iter + 1 >= kLowpMaxPasses)) {
+    bool stalled = false;
+    if (lowp) {
+      if (l2 < 0.5 * w.best32[m]) {
+        w.best32[m] = l2;
+        w.stall32[m] = 0;
+      } else {
+        w.stall32[m] += 1;
+      }
+      stalled = l2 < kLowpStallBelow && w.stall32[m] >= kLowpStall;
+    }
+    if (lowp && (flag == 2 || l2 < kLowpSwitch || stalled || iter + 1 >= kLowpMaxPasses)) {
       w.prec[m] = 1;
       w.npass32[m] = iter + 1;
     }

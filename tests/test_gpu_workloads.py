@@ -107,13 +107,13 @@ def check_workload(mols, ref, forces, min_agree):
                         # tolerance the energy carries ~5e-9 Eh of noise,
                         # 5e-6 Eh/bohr after dividing by the step
                         h = 5e-4
-                        e = {}
+                        efd = {}
                         for st in (-2, -1, 1, 2):
                             pp = pos.copy()
                             pp[at, x] += st * h
-                            e[st] = go.singlepoint(num, pp, mixer="broyden", forces=False,
-                                                   fermi_thr=1e-13).energy
-                        fd = -(8.0 * (e[1] - e[-1]) - (e[2] - e[-2])) / (12.0 * h)
+                            efd[st] = go.singlepoint(num, pp, mixer="broyden", forces=False,
+                                                     fermi_thr=1e-13).energy
+                        fd = -(8.0 * (efd[1] - efd[-1]) - (efd[2] - efd[-2])) / (12.0 * h)
                         err_engine = abs(f[a + at, x] - fd)
                         err_ref = abs(ref["forces"][a + at, x] - fd)
                         assert err_engine < 1e-6 and err_engine < err_ref, (k, err_engine, err_ref)
