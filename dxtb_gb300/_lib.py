@@ -23,8 +23,10 @@ EXPORTED = (
     "gbxtb_version", "gbxtb_last_error", "gbxtb_ctx_create", "gbxtb_ctx_destroy",
     "gbxtb_plan_create", "gbxtb_plan_destroy", "gbxtb_plan_sizes", "gbxtb_integrals",
     "gbxtb_singlepoint", "gbxtb_get_status", "gbxtb_get_shell_potential", "gbxtb_get_profile",
-    "gbxtb_fp64_peak", "gbxtb_get_fp32_passes",
+    "gbxtb_fp64_peak", "gbxtb_get_fp32_passes", "gbxtb_singlepoint_noalloc",
 )
+
+NOALLOC_SCRATCH_BYTES = 32 * 1024 * 1024  # GBXTB_NOALLOC_SCRATCH_BYTES
 
 PROF_CLASSES = ("atoms", "shellpairs", "cholesky", "fock", "tridiag", "bisect", "fermi", "invit",
                 "backtransform", "density", "mix", "forces")
@@ -94,12 +96,13 @@ def load() -> C.CDLL:
     lib.gbxtb_get_status.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
     lib.gbxtb_get_shell_potential.argtypes = [vp, C.POINTER(C.c_double)]
     lib.gbxtb_get_fp32_passes.argtypes = [vp, C.POINTER(C.c_int32)]
+    lib.gbxtb_singlepoint_noalloc.argtypes = [vp, C.POINTER(Options), vp, vp, vp, vp, vp]
     lib.gbxtb_fp64_peak.argtypes = [C.POINTER(C.c_double)]
     lib.gbxtb_fp64_peak.restype = C.c_int
     lib.gbxtb_get_profile.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     for name in ("gbxtb_ctx_create", "gbxtb_plan_create", "gbxtb_plan_sizes", "gbxtb_integrals",
                  "gbxtb_singlepoint", "gbxtb_get_status", "gbxtb_get_shell_potential", "gbxtb_get_profile",
-                 "gbxtb_get_fp32_passes"):
+                 "gbxtb_get_fp32_passes", "gbxtb_singlepoint_noalloc"):
         getattr(lib, name).restype = C.c_int
     _lib = lib
     return lib

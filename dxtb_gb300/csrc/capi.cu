@@ -160,6 +160,11 @@ Work make_work(const DevPlan &pl, void *base) {
 
 }  // namespace
 
+namespace gbxtb {
+int set_error(int code, const std::string &msg) { return fail(code, msg); }
+size_t plan_workspace_bytes(const gbxtb_plan *plan) { return plan ? plan->ws_bytes : 0; }
+}  // namespace gbxtb
+
 extern "C" {
 
 int gbxtb_version(void) { return GBXTB_VERSION; }

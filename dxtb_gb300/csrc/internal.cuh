@@ -10,6 +10,7 @@
 #pragma once
 
 #include <cstdint>
+#include <string>
 #include <cuda_runtime.h>
 
 #include "../../include/gbxtb.h"
@@ -205,5 +206,11 @@ void launch_energies(const DevParams &p, const DevPlan &pl, const Work &w, doubl
                      double *energy_out, double *charges_out, cudaStream_t s);
 void launch_forces(const DevParams &p, const DevPlan &pl, const Work &w, const double *pos,
                    double *grad_out, cudaStream_t s);
+
+// C-ABI helpers shared by the entry-point translation units (capi.cu):
+// record the message of a failure for gbxtb_last_error and return `code`;
+// the device scratch a plan's gbxtb_singlepoint needs.
+int set_error(int code, const std::string &msg);
+size_t plan_workspace_bytes(const gbxtb_plan *plan);
 
 }  // namespace gbxtb

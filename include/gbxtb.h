@@ -183,6 +183,31 @@ GBXTB_API int gbxtb_get_profile(gbxtb_plan *plan, double *ms, int64_t *launches,
  * over the 2l+1 orbitals of each shell.  Synchronises that call's stream. */
 GBXTB_API int gbxtb_get_shell_potential(gbxtb_plan *plan, double *potential);
 
+/* Device scratch compiled into the library for gbxtb_singlepoint_noalloc. */
+#define GBXTB_NOALLOC_SCRATCH_BYTES ((size_t)32 * 1024 * 1024)
+
+/* gbxtb_singlepoint for callers that cannot allocate device memory.
+ * It has no counterpart in the reference, whose PyTorch path allocates as it
+ * goes.  Some callers cannot do that when they compute: for example, a host
+ * framework whose memory pool must not grow once it is set up, a real-time
+ * loop that forbids cudaMalloc after start-up, or a plugin callback that is
+ * given only a stream.  This entry point takes no workspace.  Its scratch is
+ * a fixed device array of GBXTB_NOALLOC_SCRATCH_BYTES inside the library,
+ * which every GPU that loads the library holds until the process exits.  It
+ * calls no cudaMalloc, cudaFree or allocating library routine.  The caller
+ * still owns the positions and outputs (same meaning as gbxtb_singlepoint).
+ * Limits and rules:
+ *   - plans whose workspace_bytes (gbxtb_plan_create) exceed the array are
+ *     rejected with GBXTB_ERR_WORKSPACE; opts->profile must be 0;
+ *   - the first call on a device looks up the array's device address (with
+ *     that device current); make that first call before any stream capture;
+ *   - all calls share the one array, which keeps the last call's contents
+ *     (the driver clears what it reads first): calls whose GPU work overlaps,
+ *     on other streams or threads, race on it and must be serialised. */
+GBXTB_API int gbxtb_singlepoint_noalloc(gbxtb_plan *plan, const gbxtb_options *opts,
+                                        const double *positions_dev, double *energy_dev,
+                                        double *charges_dev, double *gradient_dev, void *stream);
+
 /* Measured FP64 FMA throughput of the current device in GFLOP/s (a short
  * microbenchmark, ~10 ms); used as the roofline denominator of the
  * FP64-bound kernels.  No counterpart in the reference. */
