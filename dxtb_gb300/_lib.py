@@ -24,6 +24,9 @@ EXPORTED = (
     "gbxtb_plan_create", "gbxtb_plan_destroy", "gbxtb_plan_sizes", "gbxtb_integrals",
     "gbxtb_singlepoint", "gbxtb_get_status", "gbxtb_get_shell_potential", "gbxtb_get_profile",
     "gbxtb_fp64_peak", "gbxtb_get_fp32_passes", "gbxtb_singlepoint_noalloc",
+    "gbxtb_pool_create", "gbxtb_pool_destroy", "gbxtb_pool_free_slots", "gbxtb_pool_admit",
+    "gbxtb_pool_step_launch", "gbxtb_pool_step_finish", "gbxtb_pool_result", "gbxtb_pool_step_poll",
+    "gbxtb_plan_autotune",
 )
 
 NOALLOC_SCRATCH_BYTES = 32 * 1024 * 1024  # GBXTB_NOALLOC_SCRATCH_BYTES
@@ -97,12 +100,26 @@ def load() -> C.CDLL:
     lib.gbxtb_get_shell_potential.argtypes = [vp, C.POINTER(C.c_double)]
     lib.gbxtb_get_fp32_passes.argtypes = [vp, C.POINTER(C.c_int32)]
     lib.gbxtb_singlepoint_noalloc.argtypes = [vp, C.POINTER(Options), vp, vp, vp, vp, vp]
+    i32p, f64p = C.POINTER(C.c_int32), C.POINTER(C.c_double)
+    lib.gbxtb_pool_create.argtypes = [vp, C.POINTER(Options), C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                      C.POINTER(vp), C.POINTER(C.c_size_t)]
+    lib.gbxtb_pool_destroy.argtypes = [vp]
+    lib.gbxtb_pool_destroy.restype = None
+    lib.gbxtb_pool_free_slots.argtypes = [vp]
+    lib.gbxtb_pool_admit.argtypes = [vp, C.c_int32, i32p, f64p, C.c_double, C.c_int32, i32p]
+    lib.gbxtb_pool_step_launch.argtypes = [vp, vp]
+    lib.gbxtb_pool_step_poll.argtypes = [vp]
+    lib.gbxtb_plan_autotune.argtypes = [vp, C.POINTER(Options), vp, vp, C.c_size_t, vp, C.POINTER(C.c_int32)]
+    lib.gbxtb_pool_step_finish.argtypes = [vp, i32p, i32p, i32p]
+    lib.gbxtb_pool_result.argtypes = [vp, C.c_int32, f64p, f64p, f64p, i32p, i32p]
     lib.gbxtb_fp64_peak.argtypes = [C.POINTER(C.c_double)]
     lib.gbxtb_fp64_peak.restype = C.c_int
     lib.gbxtb_get_profile.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     for name in ("gbxtb_ctx_create", "gbxtb_plan_create", "gbxtb_plan_sizes", "gbxtb_integrals",
                  "gbxtb_singlepoint", "gbxtb_get_status", "gbxtb_get_shell_potential", "gbxtb_get_profile",
-                 "gbxtb_get_fp32_passes", "gbxtb_singlepoint_noalloc"):
+                 "gbxtb_get_fp32_passes", "gbxtb_singlepoint_noalloc", "gbxtb_pool_create",
+                 "gbxtb_pool_free_slots", "gbxtb_pool_admit", "gbxtb_pool_step_launch",
+                 "gbxtb_pool_step_finish", "gbxtb_pool_result", "gbxtb_pool_step_poll", "gbxtb_plan_autotune"):
         getattr(lib, name).restype = C.c_int
     _lib = lib
     return lib

@@ -57,6 +57,7 @@ DEFAULT_OPTS = {
     "verbosity": 0,
     "profile": False,        # per-stage device timings (last_profile)
     "mixed_precision": True,  # FP32 linear algebra in the early SCF passes
+    "autotune": "auto",      # tune eigensolver launch shapes on the first call (auto: batches of >= 32)
 }
 _ACCEPTED_IGNORED = {"scf_mode", "scp_mode", "int_driver", "int_level", "batch_mode", "damp",
                      "damp_init", "mix_guess", "cache_enabled", "timer", "strict", "log_level"}
@@ -132,6 +133,7 @@ class Plan:
         self.sizes = sizes
         self.device = ctx.device
         self._ws: torch.Tensor | None = None
+        self.tuned: list | None = None  # autotuned launch shapes, once tuned
 
     def workspace(self) -> torch.Tensor:
         if self._ws is None:
@@ -280,6 +282,13 @@ class GFN1Calculator:
         ws = plan.workspace()
         opt = self._options(forces)
         stream = torch.cuda.current_stream(dev).cuda_stream
+        tune = self.opts["autotune"]
+        if plan.tuned is None and (tune is True or (tune == "auto" and plan.nmol >= 32)):
+            choice = np.zeros(4, dtype=np.int32)
+            with torch.cuda.device(dev):
+                _lib.check(lib.gbxtb_plan_autotune(plan.handle, C.byref(opt), pos.data_ptr(), ws.data_ptr(),
+                                                   plan.ws_bytes, stream, _lib.ptr(choice, C.c_int32)))
+            plan.tuned = choice.tolist()
         with torch.cuda.device(dev):
             _lib.check(lib.gbxtb_singlepoint(
                 plan.handle, C.byref(opt), pos.data_ptr(), energy.data_ptr(), charges.data_ptr(),

@@ -9,7 +9,7 @@
 //   SCF driver    scf/unrolling/default.py:71-136 (iterate potential,
 //                 mix, stop on convergence or maxiter, final charges from the
 //                 last unmixed potential), calculators/types/energy.py:78-402
-#include "internal.cuh"
+#include "engine.h"
 
 #include <algorithm>
 #include <cmath>
@@ -19,29 +19,13 @@
 #include <string>
 #include <vector>
 
-namespace gbxtb {
-void launch_gemm(const DevPlan &pl, const Work &w, const int64_t *tile0, int64_t ntile, int mode,
-                 int all, cudaStream_t s);
-void launch_tridiag(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s);
-void launch_lowp_copies(const DevPlan &pl, const Work &w, cudaStream_t s);
-void launch_tridiag_smem(const DevPlan &pl, const Work &w, cudaStream_t s);
-void launch_tridiag_cluster(const DevPlan &pl, const Work &w, const int32_t *mol_list, int count,
-                            int maxn, cudaStream_t s);
-void launch_bisect(const DevPlan &pl, const Work &w, int maxn, double kt, const int32_t *mol_list, int count,
-                   int threads, cudaStream_t s);
-void launch_invit(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s);
-void launch_backtransform(const DevPlan &pl, const Work &w, int maxn, const int32_t *mol_list, int count,
-                          cudaStream_t s);
-cudaError_t set_linalg_smem_limits(int maxn);
-void launch_count_active(const DevPlan &pl, const Work &w, cudaStream_t s);
-}  // namespace gbxtb
-
 using namespace gbxtb;
 
 namespace {
-
 thread_local std::string g_err;
+}  // namespace
 
+namespace gbxtb {
 int fail(int code, const std::string &msg) {
   g_err = msg;
   return code;
@@ -51,116 +35,56 @@ int cuda_fail(cudaError_t e, const char *what) {
   g_err = std::string(what) + ": " + cudaGetErrorString(e);
   return GBXTB_ERR_CUDA;
 }
-
-#define CK(call)                                  \
-  do {                                            \
-    cudaError_t e__ = (call);                     \
-    if (e__ != cudaSuccess) return cuda_fail(e__, #call); \
-  } while (0)
-
-size_t align256(size_t x) { return (x + 255) / 256 * 256; }
-
-constexpr int kHistMax = 29;
-
-}  // namespace
-
-struct gbxtb_ctx {
-  int device = 0;
-  DevParams p{};
-  void *dbuf = nullptr;
-  std::vector<int32_t> elem_shell0, elem_nshell, shell_int;
-  std::vector<double> shell_data, elem_data;
-};
-
-struct gbxtb_plan {
-  gbxtb_ctx *ctx = nullptr;
-  DevPlan pl{};
-  int64_t *tile0 = nullptr;
-  int64_t ntile = 0;
-  int maxn = 0;
-  void *dbuf = nullptr;
-  size_t ws_bytes = 0;
-  std::vector<MolDesc> mol;
-  // state of the last singlepoint
-  cudaStream_t last_stream = nullptr;
-  Work last_work{};
-  bool has_run = false;
-  int32_t *h_active = nullptr;  // pinned
-  int num_sms = 0;
-  int smem_launches = 0;  // size classes with molecules (k_tridiag_smem launches per pass)
-  // profiling
-  cudaEvent_t ev[GBXTB_PROF_CLASSES][2] = {};
-  bool ev_ready = false;
-  double prof_ms[GBXTB_PROF_CLASSES] = {};
-  int64_t prof_launches[GBXTB_PROF_CLASSES] = {};
-  int64_t total_launches = 0;
-};
-
-namespace {
-
-// Workspace layout of a plan.
-struct Layout {
-  size_t off[64];
-  int n = 0;
-  size_t total = 0;
-  size_t add(size_t bytes) {
-    off[n] = total;
-    total += align256(bytes);
-    return off[n++];
-  }
-};
-
-Layout make_layout(const DevPlan &pl) {
-  Layout L;
-  const size_t d = sizeof(double), i4 = sizeof(int32_t);
-  for (int k = 0; k < 8; ++k) L.add(d * pl.nmat);          // S H0 Linv A Z P H0p lo
-  L.add(d * 5 * pl.nmat);                                   // invit
-  for (int k = 0; k < 6; ++k) L.add(d * pl.nao);            // eig d e tau q ldiag
-  L.add(d * 2 * pl.nao);                                    // occ
-  for (int k = 0; k < 7; ++k) L.add(d * pl.nsh);            // qsh vin vout vmix fprev xprev dedh
-  L.add(d * kHistMax * pl.nsh);                             // hist_df
-  L.add(d * kHistMax * pl.nsh);                             // hist_u
-  L.add(d * pl.ngam);                                       // gam
-  for (int k = 0; k < 4; ++k) L.add(d * pl.natom);          // cn erep qat dedcn
-  L.add(d * 3 * pl.natom);                                  // grad
-  for (int k = 0; k < 8; ++k) L.add(i4 * pl.nmol);          // status phase iter kvec nhist prec npass32 stall32
-  L.add(d * 2 * pl.nmol);                                   // efermi
-  L.add(d * 6 * pl.nmol);                                   // energy
-  L.add(d * 2 * pl.nmol);                                   // resid
-  L.add(d * pl.nmol);                                       // best32
-  L.add(i4 * 4);                                            // active
-  L.add(i4 * pl.nmol);                                      // active_list
-  return L;
-}
-
-Work make_work(const DevPlan &pl, void *base) {
-  Layout L = make_layout(pl);
-  char *b = static_cast<char *>(base);
-  int k = 0;
-  auto D = [&]() { return reinterpret_cast<double *>(b + L.off[k++]); };
-  auto I = [&]() { return reinterpret_cast<int32_t *>(b + L.off[k++]); };
-  Work w{};
-  w.S = D(); w.H0 = D(); w.Linv = D(); w.A = D(); w.Z = D(); w.P = D(); w.H0p = D(); w.lo = D();
-  w.invit = D();
-  w.eig = D(); w.d = D(); w.e = D(); w.tau = D(); w.q = D(); w.ldiag = D();
-  w.occ = D();
-  w.qsh = D(); w.vin = D(); w.vout = D(); w.vmix = D(); w.fprev = D(); w.xprev = D(); w.dedh = D();
-  w.hist_df = D(); w.hist_u = D();
-  w.gam = D();
-  w.cn = D(); w.erep = D(); w.qat = D(); w.dedcn = D();
-  w.grad = D();
-  w.status = I(); w.phase = I(); w.iter = I(); w.kvec = I(); w.nhist = I(); w.prec = I();
-  w.npass32 = I();
-  w.stall32 = I();
-  w.efermi = D(); w.energy = D(); w.resid = D(); w.best32 = D();
-  w.active = I();
-  w.active_list = I();
-  return w;
-}
-
-}  // namespace
+}  // namespace gbxtb
 
 namespace gbxtb {
+int describe_molecule(const gbxtb_ctx *ctx, const int32_t *numbers, int natoms, double charge, int uhf,
+                      MolMaps &mm) {
+  mm = MolMaps();
+  double n0sum = 0.0;
+  for (int a = 0; a < natoms; ++a) {
+    const int z = numbers[a];
+    if (z < 1 || z > ctx->p.max_z || ctx->elem_nshell[z] < 1)
+      return fail(GBXTB_ERR_ELEMENT, "atomic number " + std::to_string(z) + " has no GFN1 parameters");
+    mm.atom_z.push_back(z);
+    mm.atom_sh0.push_back(mm.nsh);
+    mm.atom_nsh.push_back(ctx->elem_nshell[z]);
+    for (int s = 0; s < ctx->elem_nshell[z]; ++s) {
+      const int rec = ctx->elem_shell0[z] + s;
+      const int l = ctx->shell_int[(size_t)rec * GBXTB_SHELL_INTS];
+      const double refocc = ctx->shell_data[(size_t)rec * GBXTB_SHELL_DOUBLES + 19];
+      mm.sh_atom.push_back(a);
+      mm.sh_rec.push_back(rec);
+      mm.sh_ao.push_back(mm.nao);
+      mm.sh_l.push_back(l);
+      for (int k = 0; k < 2 * l + 1; ++k) {
+        mm.ao_sh.push_back(mm.nsh);
+        mm.ao_n0.push_back(refocc / (2 * l + 1));
+        n0sum += refocc / (2 * l + 1);
+      }
+      mm.nao += 2 * l + 1;
+      mm.nsh += 1;
+    }
+  }
+  mm.natom = natoms;
+  // electrons (scf/iterator.py:183-187, filling.py:41-113)
+  const double nel = std::nearbyint(n0sum - charge);
+  if (nel < 0.0) return fail(GBXTB_ERR_ARG, "negative number of electrons");
+  const int nel_i = (int)nel;
+  int u;
+  if (uhf >= 0) {
+    u = uhf;
+    if (u > nel_i) return fail(GBXTB_ERR_ARG, "more unpaired electrons than electrons");
+    if ((u % 2) != (nel_i % 2)) return fail(GBXTB_ERR_ARG, "parity of unpaired electrons and electrons differs");
+  } else {
+    u = nel_i % 2;
+  }
+  const double nb = (nel - u) / 2.0;
+  mm.nel[0] = nb + u;
+  mm.nel[1] = nb;
+  return GBXTB_OK;
+}
+
 int set_error(int code, const std::string &msg) { return fail(code, msg); }
 size_t plan_workspace_bytes(const gbxtb_plan *plan) { return plan ? plan->ws_bytes : 0; }
 }  // namespace gbxtb
@@ -251,42 +175,37 @@ int gbxtb_plan_create(gbxtb_ctx *ctx, int32_t nmol, const int32_t *numbers,
   for (int m = 0; m < nmol; ++m) {
     const int64_t a0 = atom_offsets[m], a1 = atom_offsets[m + 1];
     if (a1 <= a0) return fail(GBXTB_ERR_ARG, "molecule without atoms");
+    MolMaps mm;
+    const int rc = describe_molecule(ctx, numbers + a0, (int)(a1 - a0), charge ? charge[m] : 0.0,
+                                     (uhf && uhf[m] >= 0) ? uhf[m] : -1, mm);
+    if (rc) return rc;
     MolDesc &md = mol[m];
     md.atom0 = (int32_t)atom_z.size();
-    md.natom = (int32_t)(a1 - a0);
+    md.natom = mm.natom;
     md.sh0 = (int32_t)sh_atom.size();
     md.ao0 = (int32_t)ao_sh.size();
-    int nao = 0;
-    double n0sum = 0.0;
-    for (int64_t a = a0; a < a1; ++a) {
-      const int z = numbers[a];
-      if (z < 1 || z > ctx->p.max_z || ctx->elem_nshell[z] < 1)
-        return fail(GBXTB_ERR_ELEMENT, "atomic number " + std::to_string(z) + " has no GFN1 parameters");
-      const int ga = (int32_t)atom_z.size();
-      atom_z.push_back(z);
+    md.nsh = mm.nsh;
+    md.nao = mm.nao;
+    md.nel[0] = mm.nel[0];
+    md.nel[1] = mm.nel[1];
+    for (int a = 0; a < mm.natom; ++a) {
+      atom_z.push_back(mm.atom_z[a]);
       atom_mol.push_back(m);
-      atom_sh0.push_back((int32_t)sh_atom.size());
-      atom_nsh.push_back(ctx->elem_nshell[z]);
-      for (int s = 0; s < ctx->elem_nshell[z]; ++s) {
-        const int rec = ctx->elem_shell0[z] + s;
-        const int l = ctx->shell_int[(size_t)rec * GBXTB_SHELL_INTS];
-        const double refocc = ctx->shell_data[(size_t)rec * GBXTB_SHELL_DOUBLES + 19];
-        const int gs = (int32_t)sh_atom.size();
-        sh_atom.push_back(ga);
-        sh_rec.push_back(rec);
-        sh_ao.push_back(nao);
-        sh_l.push_back(l);
-        sh_mol.push_back(m);
-        for (int k = 0; k < 2 * l + 1; ++k) {
-          ao_sh.push_back(gs);
-          ao_n0.push_back(refocc / (2 * l + 1));
-          n0sum += refocc / (2 * l + 1);
-        }
-        nao += 2 * l + 1;
-      }
+      atom_sh0.push_back(md.sh0 + mm.atom_sh0[a]);
+      atom_nsh.push_back(mm.atom_nsh[a]);
     }
-    md.nsh = (int32_t)sh_atom.size() - md.sh0;
-    md.nao = nao;
+    for (int k = 0; k < mm.nsh; ++k) {
+      sh_atom.push_back(md.atom0 + mm.sh_atom[k]);
+      sh_rec.push_back(mm.sh_rec[k]);
+      sh_ao.push_back(mm.sh_ao[k]);
+      sh_l.push_back(mm.sh_l[k]);
+      sh_mol.push_back(m);
+    }
+    for (int k = 0; k < mm.nao; ++k) {
+      ao_sh.push_back(md.sh0 + mm.ao_sh[k]);
+      ao_n0.push_back(mm.ao_n0[k]);
+    }
+    const int nao = mm.nao;
     md.mat0 = nmat;
     md.gam0 = ngam;
     md.pair0 = npair;
@@ -297,23 +216,6 @@ int gbxtb_plan_create(gbxtb_ctx *ctx, int32_t nmol, const int32_t *numbers,
     const int64_t nt = (nao + 63) / 64;
     ntile += nt * nt;
     maxn = std::max(maxn, nao);
-    // electrons (scf/iterator.py:183-187, filling.py:41-113)
-    const double chg = charge ? charge[m] : 0.0;
-    const double nel = std::nearbyint(n0sum - chg);
-    if (nel < 0.0) return fail(GBXTB_ERR_ARG, "negative number of electrons");
-    const int nel_i = (int)nel;
-    int u;
-    if (uhf && uhf[m] >= 0) {
-      u = uhf[m];
-      if (u > nel_i) return fail(GBXTB_ERR_ARG, "more unpaired electrons than electrons");
-      if ((u % 2) != (nel_i % 2))
-        return fail(GBXTB_ERR_ARG, "parity of unpaired electrons and electrons differs");
-    } else {
-      u = nel_i % 2;
-    }
-    const double nb = (nel - u) / 2.0;
-    md.nel[0] = nb + u;
-    md.nel[1] = nb;
   }
   tile0[nmol] = ntile;
   // shared-memory size classes of the FP32 tridiagonalisation
@@ -399,7 +301,9 @@ int gbxtb_plan_create(gbxtb_ctx *ctx, int32_t nmol, const int32_t *numbers,
     d.bin_mols[c] = (const int32_t *)(b + o_bin[c]);
     d.bin_count[c] = (int)bins[c].size();
     d.bin_maxn[c] = bin_maxn[c];
+    d.bin_warps[c] = kSmemBinWarps[c];
   }
+  d.bisect_threads = 256;
   e = set_linalg_smem_limits(maxn);
   if (e != cudaSuccess) {
     cudaFree(pl->dbuf);
@@ -418,6 +322,7 @@ int gbxtb_plan_create(gbxtb_ctx *ctx, int32_t nmol, const int32_t *numbers,
     cudaDeviceGetAttribute(&pl->num_sms, cudaDevAttrMultiProcessorCount, dev);
   }
   for (int c = 0; c < kSmemBins; ++c) pl->smem_launches += bins[c].empty() ? 0 : 1;
+  for (int m = 0; m < nmol; ++m) pl->nbig += (mol[m].nao > kClusterMinN) ? 1 : 0;
   pl->ws_bytes = make_layout(d).total;
   *workspace_bytes = pl->ws_bytes;
   *out = pl;
@@ -426,6 +331,9 @@ int gbxtb_plan_create(gbxtb_ctx *ctx, int32_t nmol, const int32_t *numbers,
 
 void gbxtb_plan_destroy(gbxtb_plan *plan) {
   if (!plan) return;
+  for (int g = 0; g < 2; ++g)
+    if (plan->pass_graph[g]) cudaGraphExecDestroy(plan->pass_graph[g]);
+  if (plan->capture_stream) cudaStreamDestroy(plan->capture_stream);
   if (plan->ev_ready)
     for (int c = 0; c < GBXTB_PROF_CLASSES; ++c)
       for (int k = 0; k < 2; ++k) cudaEventDestroy(plan->ev[c][k]);
@@ -501,6 +409,111 @@ struct Prof {
 };
 }  // namespace
 
+namespace {
+// Reset the SCF state and enqueue the geometry terms of a call.
+int enqueue_setup(gbxtb_plan *plan, const Work &w, const gbxtb_options &o, const double *positions_dev,
+                  cudaStream_t s, Prof &pf) {
+  const DevPlan &pl = plan->pl;
+  const DevParams &p = plan->ctx->p;
+  const gbxtb_options *opts = &o;
+  // reset state
+  CK(cudaMemsetAsync(w.status, 0, sizeof(int32_t) * pl.nmol, s));
+  CK(cudaMemsetAsync(w.phase, 0, sizeof(int32_t) * pl.nmol, s));
+  CK(cudaMemsetAsync(w.iter, 0, sizeof(int32_t) * pl.nmol, s));
+  CK(cudaMemsetAsync(w.kvec, 0, sizeof(int32_t) * pl.nmol, s));
+  CK(cudaMemsetAsync(w.nhist, 0, sizeof(int32_t) * pl.nmol, s));
+  CK(cudaMemsetAsync(w.npass32, 0, sizeof(int32_t) * pl.nmol, s));
+  CK(cudaMemsetAsync(w.stall32, 0, sizeof(int32_t) * pl.nmol, s));
+  CK(cudaMemsetAsync(w.best32, 0x7f, sizeof(double) * pl.nmol, s));  // 1.4e306: no pass yet
+  // 0: the first passes run in FP32; any non-zero byte pattern means FP64
+  CK(cudaMemsetAsync(w.prec, opts->mixed_precision ? 0 : 1, sizeof(int32_t) * pl.nmol, s));
+  CK(cudaMemsetAsync(w.vin, 0, sizeof(double) * pl.nsh, s));
+  CK(cudaMemsetAsync(w.energy, 0, sizeof(double) * 6 * pl.nmol, s));
+  // geometry-dependent terms
+  pf.begin(GBXTB_PROF_ATOMS);
+  launch_atoms(p, pl, w, positions_dev, opts->want_forces != 0, s);
+  pf.end(GBXTB_PROF_ATOMS, 1);
+  pf.begin(GBXTB_PROF_SHELLPAIRS);
+  launch_shellpairs(p, pl, w, positions_dev, s);
+  pf.end(GBXTB_PROF_SHELLPAIRS, 1);
+  pf.begin(GBXTB_PROF_CHOLESKY);
+  const int nchol = launch_cholesky(pl, w, plan->maxn, s);
+  // H0' = L^-1 H0 L^-T once per geometry (the potential is still zero)
+  launch_gemm(pl, w, plan->tile0, plan->ntile, 0, 0, s);
+  launch_gemm(pl, w, plan->tile0, plan->ntile, 5, 0, s);
+  if (opts->mixed_precision) launch_lowp_copies(pl, w, s);
+  pf.end(GBXTB_PROF_CHOLESKY, nchol + (opts->mixed_precision ? 3 : 2));
+  CK(cudaGetLastError());
+  return GBXTB_OK;
+}
+}  // namespace
+
+namespace {
+// Enqueue one SCF pass on stream s: lists of iterating molecules at most
+// `active` long (tail shapes), large FP64 passes at most `big64`.  Returns
+// the number of kernel launches; times kernel classes when pf is given.
+int enqueue_pass(gbxtb_plan *plan, const Work &w, const gbxtb_options &o, bool tail, int active, int big64,
+                 cudaStream_t s, Prof *pf) {
+  const DevPlan &pl = plan->pl;
+  const DevParams &p = plan->ctx->p;
+  const gbxtb_options *opts = &o;
+  const int it = 0;
+  Prof none{plan, s, false};
+  Prof &prof = pf ? *pf : none;
+  const int64_t before = plan->total_launches;
+  prof.begin(GBXTB_PROF_FOCK);
+  launch_gemm(pl, w, plan->tile0, plan->ntile, 6, 0, s);
+  prof.end(GBXTB_PROF_FOCK, 1);
+  prof.begin(GBXTB_PROF_TRIDIAG);
+  // FP32 passes in shared memory, except large molecules in the tail
+  if (opts->mixed_precision) launch_tridiag_smem(pl, w, s);
+  int ntrd = opts->mixed_precision ? plan->smem_launches : 0;
+  if (tail) {
+    launch_tridiag_cluster(pl, w, w.active_list, active, plan->maxn, s);
+    ntrd += 1;
+  } else {
+    // large FP64 passes on 8-SM clusters, the rest one CTA per molecule
+    if (big64 > 0) {
+      launch_tridiag_cluster(pl, w, w.big64_list, big64, plan->maxn, s);
+      ntrd += 1;
+    }
+    launch_tridiag(pl, w, plan->maxn, s);
+    ntrd += 1;
+  }
+  prof.end(GBXTB_PROF_TRIDIAG, ntrd);
+  prof.begin(GBXTB_PROF_BISECT);
+  if (tail)
+    launch_bisect(pl, w, plan->maxn, opts->kt, w.active_list, active, 32, s);
+  else
+    launch_bisect(pl, w, plan->maxn, opts->kt, nullptr, pl.nmol, pl.bisect_threads, s);
+  prof.end(GBXTB_PROF_BISECT, 1);
+  prof.begin(GBXTB_PROF_FERMI);
+  launch_fermi(pl, w, opts->kt, opts->fermi_maxiter, s);
+  prof.end(GBXTB_PROF_FERMI, 1);
+  prof.begin(GBXTB_PROF_INVIT);
+  launch_invit(pl, w, plan->maxn, s);
+  prof.end(GBXTB_PROF_INVIT, 1);
+  prof.begin(GBXTB_PROF_BACKTRANSFORM);
+  if (tail)
+    launch_backtransform(pl, w, plan->maxn, w.active_list, active, s);
+  else
+    launch_backtransform(pl, w, plan->maxn, nullptr, pl.nmol, s);
+  prof.end(GBXTB_PROF_BACKTRANSFORM, 1);
+  prof.begin(GBXTB_PROF_DENSITY);
+  launch_gemm(pl, w, plan->tile0, plan->ntile, 2, 0, s);
+  launch_gemm(pl, w, plan->tile0, plan->ntile, 3, 0, s);
+  prof.end(GBXTB_PROF_DENSITY, 2);
+  prof.begin(GBXTB_PROF_MIX);
+  launch_charges_mix(p, pl, w, *opts, it, s);
+  launch_count_active(pl, w, s);
+  prof.end(GBXTB_PROF_MIX, 2);
+  (void)it;
+  const int n = (int)(plan->total_launches - before);
+  if (!pf) plan->total_launches = before;  // counted when the graph is launched
+  return n;
+}
+}  // namespace
+
 int gbxtb_singlepoint(gbxtb_plan *plan, const gbxtb_options *opts, const double *positions_dev,
                       double *energy_dev, double *charges_dev, double *gradient_dev,
                       void *workspace_dev, size_t workspace_bytes, void *stream) {
@@ -526,84 +539,76 @@ int gbxtb_singlepoint(gbxtb_plan *plan, const gbxtb_options *opts, const double 
   }
   plan->total_launches = 0;
   Prof pf{plan, s, opts->profile != 0};
-  // reset state
-  CK(cudaMemsetAsync(w.status, 0, sizeof(int32_t) * pl.nmol, s));
-  CK(cudaMemsetAsync(w.phase, 0, sizeof(int32_t) * pl.nmol, s));
-  CK(cudaMemsetAsync(w.iter, 0, sizeof(int32_t) * pl.nmol, s));
-  CK(cudaMemsetAsync(w.kvec, 0, sizeof(int32_t) * pl.nmol, s));
-  CK(cudaMemsetAsync(w.nhist, 0, sizeof(int32_t) * pl.nmol, s));
-  CK(cudaMemsetAsync(w.npass32, 0, sizeof(int32_t) * pl.nmol, s));
-  CK(cudaMemsetAsync(w.stall32, 0, sizeof(int32_t) * pl.nmol, s));
-  CK(cudaMemsetAsync(w.best32, 0x7f, sizeof(double) * pl.nmol, s));  // 1.4e306: no pass yet
-  // 0: the first passes run in FP32; any non-zero byte pattern means FP64
-  CK(cudaMemsetAsync(w.prec, opts->mixed_precision ? 0 : 1, sizeof(int32_t) * pl.nmol, s));
-  CK(cudaMemsetAsync(w.vin, 0, sizeof(double) * pl.nsh, s));
-  CK(cudaMemsetAsync(w.energy, 0, sizeof(double) * 6 * pl.nmol, s));
-  // geometry-dependent terms
-  pf.begin(GBXTB_PROF_ATOMS);
-  launch_atoms(p, pl, w, positions_dev, opts->want_forces != 0, s);
-  pf.end(GBXTB_PROF_ATOMS, 1);
-  pf.begin(GBXTB_PROF_SHELLPAIRS);
-  launch_shellpairs(p, pl, w, positions_dev, s);
-  pf.end(GBXTB_PROF_SHELLPAIRS, 1);
-  pf.begin(GBXTB_PROF_CHOLESKY);
-  launch_cholesky(pl, w, s);
-  // H0' = L^-1 H0 L^-T once per geometry (the potential is still zero)
-  launch_gemm(pl, w, plan->tile0, plan->ntile, 0, 0, s);
-  launch_gemm(pl, w, plan->tile0, plan->ntile, 5, 0, s);
-  if (opts->mixed_precision) launch_lowp_copies(pl, w, s);
-  pf.end(GBXTB_PROF_CHOLESKY, opts->mixed_precision ? 4 : 3);
-  CK(cudaGetLastError());
+  rc = enqueue_setup(plan, w, *opts, positions_dev, s, pf);
+  if (rc) return rc;
   // SCF: maxiter mixing iterations + the first evaluation + the final pass
   const int max_loops = opts->maxiter + 3;
   int active = pl.nmol;  // molecules iterating (known after each pass)
+  int big64 = 0;         // of those, FP64 passes on a cluster
+  launch_count_active(pl, w, s);
+  CK(cudaMemcpyAsync(plan->h_active, w.active, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  big64 = plan->h_active[1];
+  plan->total_launches += 1;
+  // the passes: replayed as a CUDA graph of one pass (one graph launch and
+  // one 8-byte copy per pass), or launched one by one with per-class timing
+  // when profiling
+  const bool use_graph = !pf.on;
+  if (use_graph) {
+    const bool stale = plan->graph_ws != workspace_dev ||
+                       std::memcmp(&plan->graph_opts, opts, sizeof(gbxtb_options)) != 0;
+    if (stale) {
+      for (int g = 0; g < 2; ++g) {
+        if (plan->pass_graph[g]) cudaGraphExecDestroy(plan->pass_graph[g]);
+        plan->pass_graph[g] = nullptr;
+      }
+      plan->graph_ws = workspace_dev;
+      plan->graph_opts = *opts;
+    }
+    // captured on a stream of the plan's own: the caller's stream may be
+    // the legacy default stream, which cannot be captured; capturing runs
+    // nothing, so it needs no ordering with the caller's work
+    if (!plan->capture_stream) CK(cudaStreamCreateWithFlags(&plan->capture_stream, cudaStreamNonBlocking));
+    cudaStream_t cs = plan->capture_stream;
+    for (int g = 0; g < 2; ++g) {
+      if (plan->pass_graph[g]) continue;
+      cudaGraph_t graph = nullptr;
+      CK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+      const int nl = g ? std::min(pl.nmol, plan->num_sms) : pl.nmol;
+      const int n = enqueue_pass(plan, w, *opts, g == 1, nl, plan->nbig, cs, nullptr);
+      const cudaError_t ce =
+          cudaMemcpyAsync(plan->h_active, w.active, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, cs);
+      // end the capture on every path, so that the stream is usable again
+      const cudaError_t ee = cudaStreamEndCapture(cs, &graph);
+      if (n < 0 || ce != cudaSuccess || ee != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        if (n < 0) return n;
+        return cuda_fail(ce != cudaSuccess ? ce : ee, "pass capture");
+      }
+      const cudaError_t ge = cudaGraphInstantiate(&plan->pass_graph[g], graph, 0);
+      cudaGraphDestroy(graph);
+      if (ge != cudaSuccess) return cuda_fail(ge, "cudaGraphInstantiate");
+      plan->pass_graph_launches[g] = n;
+    }
+  }
   for (int it = 0; it < max_loops; ++it) {
-    pf.begin(GBXTB_PROF_FOCK);
-    launch_gemm(pl, w, plan->tile0, plan->ntile, 6, 0, s);
-    pf.end(GBXTB_PROF_FOCK, 1);
-    pf.begin(GBXTB_PROF_TRIDIAG);
     // fewer molecules than SMs (the tail of the batch): spread each molecule
     // over more SMs (an 8-SM cluster for the tridiagonalisation, more blocks
     // for bisection and back-transformation), working from the device-side
     // list of molecules still iterating
     const bool tail = it > 0 && active <= plan->num_sms;
-    if (opts->mixed_precision) launch_tridiag_smem(pl, w, s);
-    if (tail)
-      launch_tridiag_cluster(pl, w, w.active_list, active, plan->maxn, s);
-    else
-      launch_tridiag(pl, w, plan->maxn, s);
-    pf.end(GBXTB_PROF_TRIDIAG, opts->mixed_precision ? 1 + plan->smem_launches : 1);
-    pf.begin(GBXTB_PROF_BISECT);
-    if (tail)
-      launch_bisect(pl, w, plan->maxn, opts->kt, w.active_list, active, 32, s);
-    else
-      launch_bisect(pl, w, plan->maxn, opts->kt, nullptr, pl.nmol, 256, s);
-    pf.end(GBXTB_PROF_BISECT, 1);
-    pf.begin(GBXTB_PROF_FERMI);
-    launch_fermi(pl, w, opts->kt, opts->fermi_maxiter, s);
-    pf.end(GBXTB_PROF_FERMI, 1);
-    pf.begin(GBXTB_PROF_INVIT);
-    launch_invit(pl, w, plan->maxn, s);
-    pf.end(GBXTB_PROF_INVIT, 1);
-    pf.begin(GBXTB_PROF_BACKTRANSFORM);
-    if (tail)
-      launch_backtransform(pl, w, plan->maxn, w.active_list, active, s);
-    else
-      launch_backtransform(pl, w, plan->maxn, nullptr, pl.nmol, s);
-    pf.end(GBXTB_PROF_BACKTRANSFORM, 1);
-    pf.begin(GBXTB_PROF_DENSITY);
-    launch_gemm(pl, w, plan->tile0, plan->ntile, 2, 0, s);
-    launch_gemm(pl, w, plan->tile0, plan->ntile, 3, 0, s);
-    pf.end(GBXTB_PROF_DENSITY, 2);
-    pf.begin(GBXTB_PROF_MIX);
-    launch_charges_mix(p, pl, w, *opts, it, s);
-    launch_count_active(pl, w, s);
-    pf.end(GBXTB_PROF_MIX, 2);
+    if (use_graph) {
+      CK(cudaGraphLaunch(plan->pass_graph[tail ? 1 : 0], s));
+      plan->total_launches += plan->pass_graph_launches[tail ? 1 : 0];
+    } else {
+      enqueue_pass(plan, w, *opts, tail, active, big64, s, &pf);
+      CK(cudaMemcpyAsync(plan->h_active, w.active, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    }
     CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(plan->h_active, w.active, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     pf.harvest();
     active = plan->h_active[0];
+    big64 = plan->h_active[1];
     if (active == 0) break;
   }
   launch_energies(p, pl, w, opts->kt, energy_dev, charges_dev, s);
@@ -622,6 +627,87 @@ int gbxtb_singlepoint(gbxtb_plan *plan, const gbxtb_options *opts, const double 
   plan->last_stream = s;
   plan->last_work = w;
   plan->has_run = true;
+  return GBXTB_OK;
+}
+
+int gbxtb_plan_autotune(gbxtb_plan *plan, const gbxtb_options *opts, const double *positions_dev,
+                        void *workspace_dev, size_t workspace_bytes, void *stream, int32_t *choice) {
+  if (!opts) return fail(GBXTB_ERR_ARG, "null argument");
+  Work w;
+  int rc = prepare(plan, positions_dev, workspace_dev, workspace_bytes, w);
+  if (rc) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  DevPlan &pl = plan->pl;
+  gbxtb_options o = *opts;
+  o.mixed_precision = 1;  // the tuned kernels serve the FP32 passes
+  o.profile = 0;
+  Prof none{plan, s, false};
+  rc = enqueue_setup(plan, w, o, positions_dev, s, none);
+  if (rc) return rc;
+  // the first pass's FP32 Fock matrices are the tuning input
+  launch_gemm(pl, w, plan->tile0, plan->ntile, 6, 0, s);
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  auto time_ms = [&](auto &&launch) -> float {
+    launch();  // warm
+    cudaEventRecord(e0, s);
+    launch();
+    launch();
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    return ms;
+  };
+  // warps per CTA of the on-chip tridiagonalisation, per size class (the
+  // kernel reads its matrix from the lower triangle, which a run leaves
+  // intact, so repeated runs time the same work)
+  const int cand_w[3] = {8, 16, 32};
+  for (int c = 0; c < kSmemBins; ++c) {
+    if (pl.bin_count[c] <= 0) continue;
+    float best = 1e30f;
+    int pick = pl.bin_warps[c];
+    for (int nw : cand_w) {
+      DevPlan one = pl;
+      for (int q = 0; q < kSmemBins; ++q) one.bin_count[q] = (q == c) ? pl.bin_count[q] : 0;
+      one.bin_warps[c] = nw;
+      const float ms = time_ms([&] { launch_tridiag_smem(one, w, s); });
+      if (ms < best) {
+        best = ms;
+        pick = nw;
+      }
+    }
+    pl.bin_warps[c] = pick;
+  }
+  launch_tridiag_smem(pl, w, s);
+  // threads per CTA of the batch-wide eigenvalue search
+  {
+    const int cand_t[3] = {64, 128, 256};
+    float best = 1e30f;
+    int pick = pl.bisect_threads;
+    for (int t : cand_t) {
+      const float ms = time_ms([&] { launch_bisect(pl, w, plan->maxn, o.kt, nullptr, pl.nmol, t, s); });
+      if (ms < best) {
+        best = ms;
+        pick = t;
+      }
+    }
+    pl.bisect_threads = pick;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(s));
+  // captured passes used the old shapes
+  for (int g = 0; g < 2; ++g) {
+    if (plan->pass_graph[g]) cudaGraphExecDestroy(plan->pass_graph[g]);
+    plan->pass_graph[g] = nullptr;
+  }
+  if (choice) {
+    for (int c = 0; c < kSmemBins; ++c) choice[c] = pl.bin_warps[c];
+    choice[kSmemBins] = pl.bisect_threads;
+  }
   return GBXTB_OK;
 }
 

@@ -199,6 +199,7 @@ __device__ __forceinline__ void decode_pair(int64_t k, int n, int &i, int &j) {
 // ---------------------------------------------------------------------------
 __global__ void k_atoms(DevParams p, DevPlan pl, Work w, const double *__restrict__ pos) {
   const int m = blockIdx.x;
+  if (!geom_due(pl, w, m)) return;
   const MolDesc md = pl.mol[m];
   const double kcn = p.g[7], cn_cut = p.g[8], rep_cut = p.g[9], kexp = p.g[6];
   for (int ia = threadIdx.x; ia < md.natom; ia += blockDim.x) {
@@ -235,7 +236,10 @@ __global__ void k_shellpairs(DevParams p, DevPlan pl, Work w, const double *__re
   const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= pl.npair) return;
   const int m = find_mol_pair(pl.mol, pl.nmol, gid);
+  if (!geom_due(pl, w, m)) return;
   const MolDesc md = pl.mol[m];
+  // (pool slots reserve pairs for their capacity; the molecule may use fewer)
+  if (gid - md.pair0 >= (int64_t)md.nsh * (md.nsh + 1) / 2) return;
   int i, j;
   decode_pair(gid - md.pair0, md.nsh, i, j);
   const int si = md.sh0 + i, sj = md.sh0 + j;
@@ -325,7 +329,9 @@ __global__ void k_force_pairs(DevParams p, DevPlan pl, Work w, const double *__r
   const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= pl.npair) return;
   const int m = find_mol_pair(pl.mol, pl.nmol, gid);
+  if (!force_due(pl, w, m)) return;
   const MolDesc md = pl.mol[m];
+  if (gid - md.pair0 >= (int64_t)md.nsh * (md.nsh + 1) / 2) return;
   int i, j;
   decode_pair(gid - md.pair0, md.nsh, i, j);
   const int si = md.sh0 + i, sj = md.sh0 + j;
@@ -410,6 +416,7 @@ __global__ void k_force_pairs(DevParams p, DevPlan pl, Work w, const double *__r
 __global__ void k_force_atoms(DevParams p, DevPlan pl, Work w, const double *__restrict__ pos,
                               double *__restrict__ grad_out) {
   const int m = blockIdx.x;
+  if (!force_due(pl, w, m)) return;
   const MolDesc md = pl.mol[m];
   const double kcn = p.g[7], cn_cut = p.g[8], rep_cut = p.g[9], kexp = p.g[6];
   for (int ia = threadIdx.x; ia < md.natom; ia += blockDim.x) {

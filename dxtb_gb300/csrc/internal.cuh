@@ -21,21 +21,30 @@ constexpr int kMaxPrim = GBXTB_MAX_PRIM;
 constexpr int kMaxL = 2;
 
 // FP32 passes tridiagonalise in shared memory (packed lower triangle, one
-// CTA per molecule).  On chip fit kSmemLocalMaxN AOs: (328 * 329 / 2 +
-// 2 * 400) floats = 219 KB of the 227 KB a CTA can have; molecules up to
-// kSmemTridiagMaxN AOs first run their leading steps in global memory.
-// Molecules are launched in size classes: n <= kSmemBinN[c] with
-// kSmemBinThreads[c] threads per CTA.
-constexpr int kSmemLocalMaxN = 328;
+// CTA per molecule, kSmemBinWarps[c] warps for size class c).  On chip fit
+// kSmemLocalMaxN AOs: 300 * 301 / 2 + 5 * 400 + 32 * 300 floats = 227 KB,
+// all a CTA can have; molecules up to kSmemTridiagMaxN AOs first run their
+// leading steps in global memory.  Molecules are launched in size classes
+// n <= kSmemBinN[c] (the shared memory of a launch follows its largest).
+constexpr int kSmemLocalMaxN = 300;
 constexpr int kSmemTridiagMaxN = 400;
 constexpr int kSmemBins = 3;
 constexpr int kSmemBinN[kSmemBins] = {96, 192, kSmemTridiagMaxN};
-constexpr int kSmemBinThreads[kSmemBins] = {256, 512, 1024};
+constexpr int kSmemBinWarps[kSmemBins] = {8, 16, 32};
+// Molecules with more AOs than this are Cholesky-factorised block-wise over
+// the whole GPU (cholesky.cu) instead of in one CTA.
+constexpr int kCholBlockMinN = 192;
+
+// FP64 passes of molecules with more AOs than this tridiagonalise on an
+// 8-SM cluster (the FP64 pipe of one SM needs ~N^3 / 2 clocks)
+constexpr int kClusterMinN = 128;
 
 // molecule phases of the SCF state machine
 constexpr int kPhaseIterate = 0;  // mixing iterations
 constexpr int kPhaseFinal = 1;    // one more V -> Q pass with the unmixed potential
-constexpr int kPhaseDone = 2;
+constexpr int kPhaseDone = 2;     // finished (batch), or free slot (pool)
+constexpr int kPhaseSetup = 3;    // pool: admitted, geometry terms pending
+constexpr int kPhaseFinished = 4; // pool: converged in this step, forces pending
 
 struct MolDesc {
   int32_t atom0, natom;
@@ -62,6 +71,7 @@ struct DevParams {
 // Index maps of a planned batch (device arrays).
 struct DevPlan {
   int nmol, natom, nsh, nao;
+  int pool;  // 0: a batch solved in one call; 1: a slot pool (continuous batching)
   int64_t nmat, ngam, npair;
   const MolDesc *mol;
   const int32_t *atom_z, *atom_mol, *atom_sh0, *atom_nsh;
@@ -71,6 +81,8 @@ struct DevPlan {
   const int32_t *bin_mols[kSmemBins];  // molecules of each shared-memory size class
   int bin_count[kSmemBins];
   int bin_maxn[kSmemBins];             // largest molecule of each class
+  int bin_warps[kSmemBins];            // warps per CTA of each class (autotuned)
+  int bisect_threads;                  // threads per CTA of the batch-wide bisection (autotuned)
 };
 
 // Device scratch of one singlepoint call.
@@ -100,8 +112,9 @@ struct Work {
   double *efermi;   // [2][nmol]
   double *energy;   // [nmol][6]: total, rep, h0, es2, es3, fermi
   double *resid;    // [nmol][2]: L2, max norm of the last potential change
-  int32_t *active;  // [1]: molecules not yet done
-  int32_t *active_list;  // [nmol]: indices of those molecules
+  int32_t *active;  // [2]: molecules not yet done; of those, FP64 passes with more than kClusterMinN AOs
+  int32_t *active_list;  // [nmol]: indices of the molecules not yet done
+  int32_t *big64_list;   // [nmol]: indices of the FP64 passes with more than kClusterMinN AOs
 };
 
 // ---------------------------------------------------------------------------
@@ -187,6 +200,27 @@ __device__ __forceinline__ bool mol_running(const Work &w, int m) {
   return w.phase[m] != kPhaseDone;
 }
 
+// Molecule of entry `idx` of a device-side molecule list, or -1 past the
+// list's current length (launches over the lists of iterating molecules may
+// be sized by an upper bound of that length).
+__device__ __forceinline__ int list_mol(const Work &w, const int32_t *list, int idx) {
+  if (list == w.active_list && idx >= w.active[0]) return -1;
+  if (list == w.big64_list && idx >= w.active[1]) return -1;
+  return list[idx];
+}
+
+// Geometry kernels work on every molecule of a batch, and in a pool only on
+// the molecules admitted since the last step.
+__device__ __forceinline__ bool geom_due(const DevPlan &pl, const Work &w, int m) {
+  return !pl.pool || w.phase[m] == kPhaseSetup;
+}
+
+// Force kernels work on every molecule of a batch, and in a pool only on the
+// molecules that converged in this step.
+__device__ __forceinline__ bool force_due(const DevPlan &pl, const Work &w, int m) {
+  return !pl.pool || w.phase[m] == kPhaseFinished;
+}
+
 // ---------------------------------------------------------------------------
 // host-side launch helpers (defined in the .cu files)
 // ---------------------------------------------------------------------------
@@ -194,7 +228,9 @@ void launch_atoms(const DevParams &p, const DevPlan &pl, const Work &w, const do
                   bool forces, cudaStream_t s);
 void launch_shellpairs(const DevParams &p, const DevPlan &pl, const Work &w, const double *pos,
                        cudaStream_t s);
-void launch_cholesky(const DevPlan &pl, const Work &w, cudaStream_t s);
+// both return the number of kernel launches they made
+int launch_cholesky(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s);
+int launch_cholesky_blocked(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s);
 void launch_fock(const DevPlan &pl, const Work &w, cudaStream_t s);
 void launch_eigensolve_tridiag(const DevPlan &pl, const Work &w, cudaStream_t s);
 void launch_fermi(const DevPlan &pl, const Work &w, double kt, int maxiter, cudaStream_t s);

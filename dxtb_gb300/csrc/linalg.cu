@@ -37,6 +37,7 @@
 #include "internal.cuh"
 
 #include <cmath>
+#include <algorithm>
 #include <cooperative_groups.h>
 #include <mutex>
 
@@ -101,8 +102,10 @@ __device__ __forceinline__ int find_mol_tile(const MolDesc *mol, const int64_t *
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(512) k_cholesky(DevPlan pl, Work w) {
   const int m = blockIdx.x;
+  if (!geom_due(pl, w, m)) return;
   const MolDesc md = pl.mol[m];
   const int n = md.nao;
+  if (n > kCholBlockMinN) return;  // launch_cholesky_blocked
   double *L = w.A + md.mat0;      // work copy of S -> L
   double *X = w.Linv + md.mat0;   // L^-1
   const double *S = w.S + md.mat0;
@@ -317,11 +320,17 @@ __device__ __forceinline__ void gemm_tile(const DevPlan &pl, const Work &w, cons
 __global__ void __launch_bounds__(256) k_gemm(DevPlan pl, Work w, const int64_t *tile0, int mode, int all) {
   const int64_t t = blockIdx.x;
   const int m = find_mol_tile(pl.mol, tile0, pl.nmol, t);
+  if (mode == 0 || mode == 5) {
+    if (!geom_due(pl, w, m)) return;
+  } else if (mode == 4) {
+    if (!force_due(pl, w, m)) return;
+  }
   if (!all && w.phase[m] == kPhaseDone) return;
   const MolDesc md = pl.mol[m];
   const int n = md.nao;
   const int nt = (n + BN - 1) / BN;
   const int local = (int)(t - tile0[m]);
+  if (local >= nt * nt) return;  // pool slots reserve tiles for their capacity
   const int ti = local / nt, tj = local % nt;
   const int kvec = min(max(w.kvec[m], 0), n);
   __shared__ double sa[BK][BM + 1];
@@ -337,6 +346,7 @@ __global__ void __launch_bounds__(256) k_gemm(DevPlan pl, Work w, const int64_t 
 // FP32 copies of the L^-1 buffer (L^-1 below, L^T above the diagonal) and of
 // L^-1 H0 L^-T, once per geometry (one block per molecule).
 __global__ void __launch_bounds__(256) k_lowp_copies(DevPlan pl, Work w) {
+  if (!geom_due(pl, w, blockIdx.x)) return;
   const MolDesc md = pl.mol[blockIdx.x];
   const int64_t nn = (int64_t)md.nao * md.nao;
   float *dst = reinterpret_cast<float *>(w.lo + md.mat0);
@@ -440,7 +450,8 @@ __global__ void __launch_bounds__(kTrdThreads) k_tridiag(DevPlan pl, Work w) {
   const int m = blockIdx.x;
   if (w.phase[m] == kPhaseDone) return;
   const MolDesc md = pl.mol[m];
-  if (w.prec[m] == 0 && md.nao <= kSmemTridiagMaxN) return;  // k_tridiag_smem
+  // FP32 passes that fit run in k_tridiag_smem, large FP64 passes on a cluster
+  if (w.prec[m] == 0 ? md.nao <= kSmemTridiagMaxN : md.nao > kClusterMinN) return;
   extern __shared__ double sm[];
   __shared__ double red[32];
   if (w.prec[m])
@@ -479,7 +490,12 @@ __device__ __forceinline__ float cta_sum(float v, float *red) {
   return t;
 }
 
-__global__ void __launch_bounds__(1024) k_tridiag_smem(DevPlan pl, Work w, const int32_t *mol_list) {
+constexpr int kSmemCols = (kSmemLocalMaxN + 31) / 32;  // column slots per lane
+
+// NW warps per CTA (the size class picks it: more warps for larger molecules)
+template <int NW>
+__global__ void __launch_bounds__(NW * 32) k_tridiag_smem(DevPlan pl, Work w, const int32_t *mol_list) {
+  constexpr int kSmemWarps = NW;
   const int m = mol_list[blockIdx.x];
   if (w.phase[m] == kPhaseDone || w.prec[m] != 0) return;
   const MolDesc md = pl.mol[m];
@@ -487,79 +503,98 @@ __global__ void __launch_bounds__(1024) k_tridiag_smem(DevPlan pl, Work w, const
   const int k0 = n > kSmemLocalMaxN ? n - kSmemLocalMaxN : 0;  // steps in global memory
   const int nl = n - k0;                                        // trailing size on chip
   extern __shared__ float smf[];
-  float *Ap = smf;                     // packed lower triangle of A[k0.., k0..]
-  float *vs = smf + poff(nl);          // [n]
-  float *ps = vs + n;                  // [n]
+  float *Ap = smf;                          // packed lower triangle of A[k0.., k0..]
+  float *vb = smf + poff(nl);               // [2][n] reflectors (current, previous)
+  float *wb = vb + 2 * n;                   // [2][n] rank-2 partners
+  float *prow = wb + 2 * n;                 // [n] row part of A v
+  float *colpart = prow + n;                // [kSmemWarps][nl] column parts of A v
   __shared__ float red[4][32];
   float *Ag = mat_view<float>(w.A, md.mat0);
   double *d = w.d + md.ao0, *e = w.e + md.ao0, *tau = w.tau + md.ao0;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = NW;
   int rb = 0;  // alternating reduction buffer
 
   // leading steps on the full matrix in global memory
-  for (int k = 0; k < k0; ++k) {
-    const int m1 = n - k - 1;
-    float part = 0.f;
-    for (int t = 1 + threadIdx.x; t < m1; t += blockDim.x) {
-      const float x = Ag[(int64_t)(k + 1 + t) * n + k];
-      part += x * x;
-    }
-    const float xn2 = cta_sum(part, red[rb]);
-    rb ^= 1;
-    const float alpha = Ag[(int64_t)(k + 1) * n + k];
-    float tk = 0.f, scale = 0.f, beta = alpha;
-    if (xn2 != 0.f) {
-      beta = -copysignf(sqrtf(alpha * alpha + xn2), alpha);
-      tk = (beta - alpha) / beta;
-      scale = 1.f / (alpha - beta);
-    }
-    if (threadIdx.x == 0) {
-      d[k] = Ag[(int64_t)k * n + k];
-      e[k] = beta;
-      tau[k] = tk;
-    }
-    if (tk == 0.f) continue;  // uniform; nothing was written
-    for (int t = threadIdx.x; t < m1; t += blockDim.x)
-      vs[t] = (t == 0) ? 1.f : Ag[(int64_t)(k + 1 + t) * n + k] * scale;
-    __syncthreads();
-    for (int t = threadIdx.x; t < m1; t += blockDim.x) Ag[(int64_t)k * n + k + 1 + t] = vs[t];
-    float pv = 0.f;
-    for (int i = wid; i < m1; i += nw) {
-      const float *row = Ag + (int64_t)(k + 1 + i) * n + (k + 1);
-      float sacc = 0.f;
-      for (int j = lane; j < m1; j += 32) sacc += row[j] * vs[j];
-      sacc = warp_sum(sacc) * tk;
-      if (lane == 0) {
-        ps[i] = sacc;
-        pv += sacc * vs[i];
+  {
+    float *vs = vb, *ps = wb;
+    for (int k = 0; k < k0; ++k) {
+      const int m1 = n - k - 1;
+      float part = 0.f;
+      for (int t = 1 + threadIdx.x; t < m1; t += blockDim.x) {
+        const float x = Ag[(int64_t)(k + 1 + t) * n + k];
+        part += x * x;
       }
+      const float xn2 = cta_sum(part, red[rb]);
+      rb ^= 1;
+      const float alpha = Ag[(int64_t)(k + 1) * n + k];
+      float tk = 0.f, scale = 0.f, beta = alpha;
+      if (xn2 != 0.f) {
+        beta = -copysignf(sqrtf(alpha * alpha + xn2), alpha);
+        tk = (beta - alpha) / beta;
+        scale = 1.f / (alpha - beta);
+      }
+      if (threadIdx.x == 0) {
+        d[k] = Ag[(int64_t)k * n + k];
+        e[k] = beta;
+        tau[k] = tk;
+      }
+      if (tk == 0.f) continue;  // uniform; nothing was written
+      for (int t = threadIdx.x; t < m1; t += blockDim.x)
+        vs[t] = (t == 0) ? 1.f : Ag[(int64_t)(k + 1 + t) * n + k] * scale;
+      __syncthreads();
+      for (int t = threadIdx.x; t < m1; t += blockDim.x) Ag[(int64_t)k * n + k + 1 + t] = vs[t];
+      float pv = 0.f;
+      for (int i = wid; i < m1; i += nw) {
+        const float *row = Ag + (int64_t)(k + 1 + i) * n + (k + 1);
+        float sacc = 0.f;
+        for (int j = lane; j < m1; j += 32) sacc += row[j] * vs[j];
+        sacc = warp_sum(sacc) * tk;
+        if (lane == 0) {
+          ps[i] = sacc;
+          pv += sacc * vs[i];
+        }
+      }
+      const float K = cta_sum(pv, red[rb]);
+      rb ^= 1;
+      const float half = 0.5f * tk * K;
+      for (int i = wid; i < m1; i += nw) {
+        float *row = Ag + (int64_t)(k + 1 + i) * n + (k + 1);
+        const float vi = vs[i], wi = ps[i] - half * vs[i];
+        for (int j = lane; j < m1; j += 32) row[j] -= vi * (ps[j] - half * vs[j]) + wi * vs[j];
+      }
+      __syncthreads();
     }
-    const float K = cta_sum(pv, red[rb]);
-    rb ^= 1;
-    const float half = 0.5f * tk * K;
-    for (int i = wid; i < m1; i += nw) {
-      float *row = Ag + (int64_t)(k + 1 + i) * n + (k + 1);
-      const float vi = vs[i], wi = ps[i] - half * vs[i];
-      for (int j = lane; j < m1; j += 32) row[j] -= vi * (ps[j] - half * vs[j]) + wi * vs[j];
-    }
-    __syncthreads();
   }
 
-  // the trailing matrix on chip (lower triangle, local indices)
+  // The trailing matrix on chip (packed lower triangle, local indices).
+  // One pass over it per step: the pending rank-2 update of the previous
+  // step is applied to each element as it is read, and the updated element
+  // enters this step's A v at once (row part in the warp, column part in
+  // per-lane registers).  Column kl+1, which the next reflector needs, gets
+  // this step's update right after the step.
   for (int i = wid; i < nl; i += nw)
     for (int j = lane; j <= i; j += 32) Ap[poff(i) + j] = Ag[(int64_t)(k0 + i) * n + k0 + j];
+  for (int t = threadIdx.x; t < 2 * n; t += blockDim.x) {
+    vb[t] = 0.f;
+    wb[t] = 0.f;
+  }
   __syncthreads();
+  // squared norm of column 0 below the sub-diagonal (the first reflector)
+  float part = 0.f;
+  for (int t = 2 + threadIdx.x; t < nl; t += blockDim.x) {
+    const float x = Ap[poff(t)];
+    part += x * x;
+  }
+  float xn2 = cta_sum(part, red[rb]);
+  rb ^= 1;
+  int cur = 0;
   for (int kl = 0; kl + 2 < nl; ++kl) {
-    const int k = k0 + kl;   // global step
+    const int k = k0 + kl;  // global step
     const int m1 = nl - kl - 1;
-    float part = 0.f;
-    for (int t = 1 + threadIdx.x; t < m1; t += blockDim.x) {
-      const float x = Ap[poff(kl + 1 + t) + kl];
-      part += x * x;
-    }
-    const float xn2 = cta_sum(part, red[rb]);
-    rb ^= 1;
-    // every thread derives the reflector parameters (identical values)
+    float *vc = vb + cur * n, *wc = wb + cur * n;              // this step
+    const float *vp = vb + (cur ^ 1) * n, *wp = wb + (cur ^ 1) * n;  // pending
+    // reflector of column kl (already fully updated); every thread derives
+    // the same parameters
     const float alpha = Ap[poff(kl + 1) + kl];
     float tk = 0.f, scale = 0.f, beta = alpha;
     if (xn2 != 0.f) {
@@ -572,54 +607,101 @@ __global__ void __launch_bounds__(1024) k_tridiag_smem(DevPlan pl, Work w, const
       e[k] = beta;
       tau[k] = tk;
     }
-    if (tk == 0.f) continue;  // uniform; nothing was written
     for (int t = threadIdx.x; t < m1; t += blockDim.x) {
-      const float v = (t == 0) ? 1.f : Ap[poff(kl + 1 + t) + kl] * scale;
-      vs[t] = v;
+      const float v = (tk == 0.f) ? 0.f : ((t == 0) ? 1.f : Ap[poff(kl + 1 + t) + kl] * scale);
+      vc[kl + 1 + t] = v;
       Ag[(int64_t)k * n + k + 1 + t] = v;  // reflector for the back-transformation
     }
     __syncthreads();
-    // p = tau A22 v: lower part by rows (two rows per warp in flight) ...
-    for (int t = wid; t < m1; t += 2 * nw) {
-      const int t2 = t + nw;
-      const float *r1 = Ap + poff(kl + 1 + t) + (kl + 1);
-      const float *r2 = Ap + poff(kl + 1 + min(t2, m1 - 1)) + (kl + 1);
+    // fused pass over rows i > kl, columns kl < j <= i; a warp works on two
+    // rows at once so that their reductions overlap
+    float acc[kSmemCols];
+#pragma unroll
+    for (int c = 0; c < kSmemCols; ++c) acc[c] = 0.f;
+    const int j0 = kl + 1;
+    for (int i1 = j0 + wid; i1 < nl; i1 += 2 * nw) {
+      const int i2 = i1 + nw;
+      const bool has2 = i2 < nl;
+      float *row1 = Ap + poff(i1);
+      float *row2 = Ap + poff(has2 ? i2 : i1);
+      const float vp1 = vp[i1], wp1 = wp[i1], vc1 = vc[i1];
+      const float vp2 = has2 ? vp[i2] : 0.f, wp2 = has2 ? wp[i2] : 0.f, vc2 = has2 ? vc[i2] : 0.f;
+      const int last = has2 ? i2 : i1;  // the longer row
       float s1 = 0.f, s2 = 0.f;
-      for (int j = lane; j <= t; j += 32) s1 += r1[j] * vs[j];
-      if (t2 < m1)
-        for (int j = lane; j <= t2; j += 32) s2 += r2[j] * vs[j];
-      s1 = warp_sum(s1);
-      s2 = warp_sum(s2);
+#pragma unroll
+      for (int c = 0; c < kSmemCols; ++c) {
+        const int j = j0 + lane + 32 * c;
+        if (32 * c > last - j0) break;  // uniform over the warp
+        if (j <= last) {
+          const float wpj = wp[j], vpj = vp[j], vcj = vc[j];
+          float add = 0.f;
+          if (j <= i1) {
+            const float a = row1[j] - (vp1 * wpj + wp1 * vpj);
+            row1[j] = a;
+            s1 += a * vcj;
+            if (j < i1) add += a * vc1;
+          }
+          if (has2) {
+            const float a = row2[j] - (vp2 * wpj + wp2 * vpj);
+            row2[j] = a;
+            s2 += a * vcj;
+            if (j < i2) add += a * vc2;
+          }
+          acc[c] += add;
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+        s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+      }
       if (lane == 0) {
-        ps[t] = s1;
-        if (t2 < m1) ps[t2] = s2;
+        prow[i1] = s1;
+        if (has2) prow[i2] = s2;
       }
     }
+#pragma unroll
+    for (int c = 0; c < kSmemCols; ++c) {
+      const int j = j0 + lane + 32 * c;
+      if (j < nl) colpart[wid * nl + j] = acc[c];
+    }
     __syncthreads();
-    // ... strict upper part by columns, then K = p.v
+    // p = tau A v, K = p.v, w = p - tau K v / 2
     float pv = 0.f;
-    for (int j = wid; j < m1; j += nw) {
-      float sacc = 0.f;
-      for (int i = j + 1 + lane; i < m1; i += 32) sacc += Ap[poff(kl + 1 + i) + kl + 1 + j] * vs[i];
-      sacc = warp_sum(sacc);
-      if (lane == 0) {
-        const float pj = tk * (ps[j] + sacc);
-        ps[j] = pj;
-        pv += pj * vs[j];
-      }
+    for (int i = j0 + threadIdx.x; i < nl; i += blockDim.x) {
+      float sum = prow[i];
+#pragma unroll
+      for (int q = 0; q < kSmemWarps; ++q) sum += colpart[q * nl + i];
+      const float pi = tk * sum;
+      prow[i] = pi;
+      pv += pi * vc[i];
     }
     const float K = cta_sum(pv, red[rb]);
     rb ^= 1;
     const float half = 0.5f * tk * K;
-    // A22 -= v w^T + w v^T (lower triangle), w = p - half v
-    for (int t = wid; t < m1; t += nw) {
-      float *row = Ap + poff(kl + 1 + t) + (kl + 1);
-      const float vi = vs[t], wi = ps[t] - half * vs[t];
-      for (int j = lane; j <= t; j += 32) row[j] -= vi * (ps[j] - half * vs[j]) + wi * vs[j];
-    }
+    for (int i = j0 + threadIdx.x; i < nl; i += blockDim.x) wc[i] = prow[i] - half * vc[i];
     __syncthreads();
+    // this step's update of column kl+1 (rows i >= kl+1), and the squared
+    // norm of its entries below the sub-diagonal (the next reflector)
+    part = 0.f;
+    {
+      const float vj = vc[j0], wj = wc[j0];
+      for (int i = j0 + threadIdx.x; i < nl; i += blockDim.x) {
+        const float a = Ap[poff(i) + j0] - (vc[i] * wj + wc[i] * vj);
+        Ap[poff(i) + j0] = a;
+        if (i >= j0 + 2) part += a * a;
+      }
+    }
+    xn2 = cta_sum(part, red[rb]);
+    rb ^= 1;
+    cur ^= 1;
   }
+  // the last diagonal element still carries the final step's update
   if (threadIdx.x == 0) {
+    if (nl >= 3) {
+      const float *vp = vb + (cur ^ 1) * n, *wp = wb + (cur ^ 1) * n;
+      Ap[poff(nl - 1) + nl - 1] -= 2.f * vp[nl - 1] * wp[nl - 1];
+    }
     if (nl >= 2) {
       d[n - 2] = Ap[poff(nl - 2) + nl - 2];
       d[n - 1] = Ap[poff(nl - 1) + nl - 1];
@@ -743,7 +825,8 @@ __device__ __forceinline__ void tridiag_cluster_body(cg::cluster_group &cluster,
 __global__ void __cluster_dims__(kClusterSize, 1, 1) __launch_bounds__(kTrdClThreads)
     k_tridiag_cluster(DevPlan pl, Work w, const int32_t *mol_list) {
   cg::cluster_group cluster = cg::this_cluster();
-  const int m = mol_list[blockIdx.x / kClusterSize];
+  const int m = list_mol(w, mol_list, blockIdx.x / kClusterSize);
+  if (m < 0) return;  // the whole cluster
   const MolDesc md = pl.mol[m];
   extern __shared__ double sm[];
   __shared__ double red[32];
@@ -840,6 +923,8 @@ __device__ __forceinline__ int sturm_count(const float *ds, const float *e2, int
 }
 
 
+constexpr int kBisectGroup = 8;  // lanes per eigenvalue in the multisection
+
 // Newton correction -p_n(x) / p_n'(x) of the characteristic polynomial
 // p_n(x) = det(T - x I) of the tridiagonal (ds, e2 = e^2):
 //   p_{j+1} = (d_j - x) p_j - e_{j-1}^2 p_{j-1},
@@ -920,33 +1005,56 @@ __device__ __forceinline__ void bisect_body(const MolDesc &md, const Work &w, in
   const double piv64 = Num<double>::safemin * fmax(1.0, emax);
   // index of the lowest eigenvalue of the alpha channel that is empty at T=0
   const int lumo = min(n - 1, (int)ceil(md.nel[0] - 5.0e-15));
-  if (threadIdx.x == 0) {
+  const int lane = threadIdx.x & 31;
+  if (threadIdx.x < 32) {
+    // LUMO bracket to 1e-4 by 33-section: the warp's 32 points per round
     float lo = (float)glo32, hi = (float)ghi32;
-    for (int it = 0; it < 96 && hi - lo > 1.0e-4f; ++it) {
-      const float mid = 0.5f * (lo + hi);
-      if (sturm_count(ds32, e2_32, n, mid, piv32) <= lumo) lo = mid; else hi = mid;
+    for (int it = 0; it < 24 && hi - lo > 1.0e-4f; ++it) {
+      const float x = lo + (hi - lo) * (float)(lane + 1) / 33.0f;
+      const unsigned below = __ballot_sync(0xffffffffu, sturm_count(ds32, e2_32, n, x, piv32) <= lumo);
+      const int p = __popc(below);
+      const float nlo = (p > 0) ? lo + (hi - lo) * (float)p / 33.0f : lo;
+      const float nhi = (p < 32) ? lo + (hi - lo) * (float)(p + 1) / 33.0f : hi;
+      if (nlo == lo && nhi == hi) break;
+      lo = nlo;
+      hi = nhi;
     }
-    const double cut = (double)hi + 60.0 * kt + 0.01;
-    s_cut = cut;
-    s_ncut = max(lumo + 1, min(n, sturm_count(ds32, e2_32, n, (float)cut, piv32)));
+    if (lane == 0) {
+      const double cut = (double)hi + 60.0 * kt + 0.01;
+      s_cut = cut;
+      s_ncut = max(lumo + 1, min(n, sturm_count(ds32, e2_32, n, (float)cut, piv32)));
+    }
   }
   __syncthreads();
   const double cut = s_cut;
   const int ncut = s_ncut;
-  const int stride = blockDim.x * nsplit;
-  for (int idx = part * blockDim.x + threadIdx.x; idx < n; idx += stride) {
+  // eigenvalue idx is located by a group of kBisectGroup lanes: each round
+  // evaluates kBisectGroup Sturm counts at once and shrinks the bracket by
+  // kBisectGroup + 1 (3.2 bits per round instead of 1)
+  const int r = threadIdx.x % kBisectGroup, grp = threadIdx.x / kBisectGroup;
+  const unsigned gmask = ((1u << kBisectGroup) - 1u) << (lane & ~(kBisectGroup - 1));
+  const int per_block = blockDim.x / kBisectGroup;
+  const int stride = per_block * nsplit;
+  for (int idx = part * per_block + grp; idx < n; idx += stride) {
     if (idx >= ncut) {
-      ev[idx] = cut + 1.0 + 1.0e-3 * (idx - ncut);  // empty orbital (placeholder)
+      if (r == 0) ev[idx] = cut + 1.0 + 1.0e-3 * (idx - ncut);  // empty orbital (placeholder)
       continue;
     }
-    // FP32 bisection to the resolution of the FP32 copy (eps32 |T|)
+    // FP32 multisection to the resolution of the FP32 copy (eps32 |T|)
     const float ftol = (float)(2.0 * Num<float>::eps * tnorm);
     float lo = (float)glo32, hi = (float)fmax(cut, ghi32);
-    for (int it = 0; it < 96 && hi - lo > ftol; ++it) {
-      const float mid = 0.5f * (lo + hi);
-      if (mid <= lo || mid >= hi) break;
-      if (sturm_count(ds32, e2_32, n, mid, piv32) <= idx) lo = mid; else hi = mid;
+    constexpr float kInv = 1.0f / (kBisectGroup + 1);
+    for (int it = 0; it < 40 && hi - lo > ftol; ++it) {
+      const float x = lo + (hi - lo) * ((float)(r + 1) * kInv);
+      const unsigned below = __ballot_sync(gmask, sturm_count(ds32, e2_32, n, x, piv32) <= idx) & gmask;
+      const int p = __popc(below);
+      const float nlo = (p > 0) ? lo + (hi - lo) * ((float)p * kInv) : lo;
+      const float nhi = (p < kBisectGroup) ? lo + (hi - lo) * ((float)(p + 1) * kInv) : hi;
+      if (nlo == lo && nhi == hi) break;
+      lo = nlo;
+      hi = nhi;
     }
+    if (r != 0) continue;
     double x = 0.5 * ((double)lo + (double)hi);
     if (kFp64) {
       const double tol = 4.0 * Num<double>::eps * tnorm;
@@ -974,14 +1082,15 @@ __device__ __forceinline__ void bisect_body(const MolDesc &md, const Work &w, in
 }
 
 // grid (molecules, parts): block (x, y) handles eigenvalue indices
-// y*256 + t + j*256*parts of molecule mol_list[x] (all molecules if
-// mol_list is null)
+// y*g + t/8 + j*g*parts (g = threads/8) of molecule mol_list[x] (all
+// molecules if mol_list is null)
 __global__ void __launch_bounds__(256) k_bisect(DevPlan pl, Work w, double kt, const int32_t *mol_list) {
-  const int m = mol_list ? mol_list[blockIdx.x] : (int)blockIdx.x;
+  const int m = mol_list ? list_mol(w, mol_list, blockIdx.x) : (int)blockIdx.x;
+  if (m < 0) return;
   const int part = blockIdx.y;
   if (w.phase[m] == kPhaseDone) return;
   const MolDesc md = pl.mol[m];
-  if (part * (int)blockDim.x >= md.nao) return;  // no index of this part (uniform)
+  if (part * (int)(blockDim.x / kBisectGroup) >= md.nao) return;  // no index of this part (uniform)
   extern __shared__ double sm[];
   __shared__ double red[32];
   if (w.prec[m])
@@ -1048,30 +1157,66 @@ __device__ __forceinline__ void invit_factor(int n, int i, T lam, const T *d, co
 template <typename T>
 __device__ __forceinline__ void invit_solve(int n, int i, const T *U1, const T *U2, const T *U3, const T *LM,
                                             const T *PV, T *Y) {
-  // forward sweep with the running component in a register (no store->load
-  // dependence through memory from one step to the next)
+  // The sweeps are sequential recurrences; their operands are read in
+  // chunks of kChunk rows ahead of the arithmetic, so that one L2 round trip
+  // serves kChunk steps instead of one.
+  constexpr int kChunk = 8;
+  // forward sweep with the running component in a register
   T carry = Y[i];
-  for (int j = 0; j < n - 1; ++j) {
-    const int64_t o = (int64_t)j * n + i;
-    const T yj1 = Y[o + n];
-    const T l = LM[o];
-    if (PV[o] != T(0)) {
-      Y[o] = yj1;
-      carry = carry - l * yj1;
-    } else {
-      Y[o] = carry;
-      carry = yj1 - l * carry;
+  for (int j0 = 0; j0 < n - 1; j0 += kChunk) {
+    T yn[kChunk], ln[kChunk], pn[kChunk];
+#pragma unroll
+    for (int c = 0; c < kChunk; ++c) {
+      const int j = j0 + c;
+      if (j < n - 1) {
+        const int64_t o = (int64_t)j * n + i;
+        yn[c] = Y[o + n];
+        ln[c] = LM[o];
+        pn[c] = PV[o];
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < kChunk; ++c) {
+      const int j = j0 + c;
+      if (j < n - 1) {
+        const int64_t o = (int64_t)j * n + i;
+        if (pn[c] != T(0)) {
+          Y[o] = yn[c];
+          carry = carry - ln[c] * yn[c];
+        } else {
+          Y[o] = carry;
+          carry = yn[c] - ln[c] * carry;
+        }
+      }
     }
   }
   Y[(int64_t)(n - 1) * n + i] = carry;
+  // back substitution
   T x1 = T(0), x2 = T(0), nrm = T(0);
-  for (int j = n - 1; j >= 0; --j) {
-    const int64_t o = (int64_t)j * n + i;
-    const T s = (Y[o] - U2[o] * x1 - U3[o] * x2) / U1[o];
-    Y[o] = s;
-    x2 = x1;
-    x1 = s;
-    nrm = fmax(nrm, fabs(s));
+  for (int j0 = n - 1; j0 >= 0; j0 -= kChunk) {
+    T yv[kChunk], u1[kChunk], u2[kChunk], u3[kChunk];
+#pragma unroll
+    for (int c = 0; c < kChunk; ++c) {
+      const int j = j0 - c;
+      if (j >= 0) {
+        const int64_t o = (int64_t)j * n + i;
+        yv[c] = Y[o];
+        u1[c] = U1[o];
+        u2[c] = U2[o];
+        u3[c] = U3[o];
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < kChunk; ++c) {
+      const int j = j0 - c;
+      if (j >= 0) {
+        const T sv = (yv[c] - u2[c] * x1 - u3[c] * x2) / u1[c];
+        Y[(int64_t)j * n + i] = sv;
+        x2 = x1;
+        x1 = sv;
+        nrm = fmax(nrm, fabs(sv));
+      }
+    }
   }
   const T inv = (nrm > T(0)) ? T(1) / nrm : T(1);
   T s2 = T(0);
@@ -1218,7 +1363,8 @@ __device__ __forceinline__ void backtransform_body(const MolDesc &md, const Work
 // grid (column groups, molecules): molecule mol_list[y] (all if null)
 template <int COLS>
 __global__ void __launch_bounds__(kBtThreads) k_backtransform(DevPlan pl, Work w, const int32_t *mol_list) {
-  const int m = mol_list ? mol_list[blockIdx.y] : (int)blockIdx.y;
+  const int m = mol_list ? list_mol(w, mol_list, blockIdx.y) : (int)blockIdx.y;
+  if (m < 0) return;
   if (w.phase[m] == kPhaseDone) return;
   const MolDesc md = pl.mol[m];
   const int n = md.nao;
@@ -1279,7 +1425,8 @@ __device__ __forceinline__ void backtransform_column(const MolDesc &md, const Wo
 // every molecule has at most 32 * NQ AOs
 template <int NQ>
 __global__ void __launch_bounds__(256) k_backtransform_warp(DevPlan pl, Work w, const int32_t *mol_list) {
-  const int m = mol_list ? mol_list[blockIdx.y] : (int)blockIdx.y;
+  const int m = mol_list ? list_mol(w, mol_list, blockIdx.y) : (int)blockIdx.y;
+  if (m < 0) return;
   if (w.phase[m] == kPhaseDone) return;
   const MolDesc md = pl.mol[m];
   const int kvec = min(max(w.kvec[m], 0), md.nao);
@@ -1296,8 +1443,9 @@ __global__ void __launch_bounds__(256) k_backtransform_warp(DevPlan pl, Work w, 
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
-void launch_cholesky(const DevPlan &pl, const Work &w, cudaStream_t s) {
+int launch_cholesky(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s) {
   k_cholesky<<<pl.nmol, 512, 0, s>>>(pl, w);
+  return 1 + launch_cholesky_blocked(pl, w, maxn, s);
 }
 
 void launch_gemm(const DevPlan &pl, const Work &w, const int64_t *tile0, int64_t ntile, int mode,
@@ -1316,15 +1464,25 @@ void launch_tridiag(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s) 
 
 // FP32 passes of molecules with at most kSmemTridiagMaxN AOs, one launch
 // per size class.
+size_t tridiag_smem_bytes(int nmax, int nwarps) {
+  const int nloc = nmax < kSmemLocalMaxN ? nmax : kSmemLocalMaxN;
+  return sizeof(float) * ((size_t)nloc * (nloc + 1) / 2 + 5 * (size_t)nmax + (size_t)nwarps * nloc);
+}
+
 void launch_tridiag_smem(const DevPlan &pl, const Work &w, cudaStream_t s) {
   for (int c = 0; c < kSmemBins; ++c) {
     if (pl.bin_count[c] <= 0) continue;
-    const int nmax = pl.bin_maxn[c];
-    const int nloc = nmax < kSmemLocalMaxN ? nmax : kSmemLocalMaxN;
-    const size_t smem = sizeof(float) * ((size_t)nloc * (nloc + 1) / 2 + 2 * (size_t)nmax);
-    k_tridiag_smem<<<pl.bin_count[c], kSmemBinThreads[c], smem, s>>>(pl, w, pl.bin_mols[c]);
+    const int nw = pl.bin_warps[c] ? pl.bin_warps[c] : kSmemBinWarps[c];
+    const size_t smem = tridiag_smem_bytes(pl.bin_maxn[c], nw);
+    if (nw == 8)
+      k_tridiag_smem<8><<<pl.bin_count[c], 256, smem, s>>>(pl, w, pl.bin_mols[c]);
+    else if (nw == 16)
+      k_tridiag_smem<16><<<pl.bin_count[c], 512, smem, s>>>(pl, w, pl.bin_mols[c]);
+    else
+      k_tridiag_smem<32><<<pl.bin_count[c], 1024, smem, s>>>(pl, w, pl.bin_mols[c]);
   }
 }
+
 
 // Cluster tridiagonalisation for the molecules listed in mol_list (device).
 void launch_tridiag_cluster(const DevPlan &pl, const Work &w, const int32_t *mol_list, int count,
@@ -1341,7 +1499,8 @@ void launch_bisect(const DevPlan &pl, const Work &w, int maxn, double kt, const 
                    int threads, cudaStream_t s) {
   if (count <= 0) return;
   const size_t smem = sizeof(double) * 3 * (size_t)maxn;
-  dim3 grid(count, (maxn + threads - 1) / threads);
+  const int per_block = threads / kBisectGroup;
+  dim3 grid(count, (maxn + per_block - 1) / per_block);
   k_bisect<<<grid, threads, smem, s>>>(pl, w, kt, mol_list);
 }
 
@@ -1384,27 +1543,41 @@ void launch_backtransform(const DevPlan &pl, const Work &w, int maxn, const int3
 // wide, and plans created earlier keep launching, so it only ever grows.
 cudaError_t set_linalg_smem_limits(int maxn) {
   static std::mutex mu;
-  static size_t cur_smem = 0, cur2 = 0, cur3 = 0;
+  static size_t cur_smem = 0, cur1 = 0, cur2 = 0, cur3 = 0;
   std::lock_guard<std::mutex> lock(mu);
-  const int nb = maxn < kSmemLocalMaxN ? maxn : kSmemLocalMaxN;
-  const int nv = maxn < kSmemTridiagMaxN ? maxn : kSmemTridiagMaxN;
-  const size_t need_s = sizeof(float) * ((size_t)nb * (nb + 1) / 2 + 2 * (size_t)nv);
+  // every warp count of k_tridiag_smem may serve any size class (autotuning)
+  const size_t need_s = tridiag_smem_bytes(maxn < kSmemTridiagMaxN ? maxn : kSmemTridiagMaxN, 32);
+  const size_t need1 = sizeof(double) * (size_t)maxn;
   const size_t need2 = sizeof(double) * 2 * (size_t)maxn;
   const size_t need3 = sizeof(double) * 3 * (size_t)maxn;
+  // above 48 KB of dynamic plus static shared memory a kernel needs the
+  // attribute; the kernels' static arrays take at most 4 KB
+  const size_t opt_in = 44 * 1024;
   cudaError_t e = cudaSuccess;
-  if (need_s > 48 * 1024 && need_s > cur_smem) {
-    e = cudaFuncSetAttribute(k_tridiag_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need_s);
+  if (need_s > opt_in && need_s > cur_smem) {
+    e = cudaFuncSetAttribute(k_tridiag_smem<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need_s);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_tridiag_smem<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need_s);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_tridiag_smem<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need_s);
     if (e != cudaSuccess) return e;
     cur_smem = need_s;
   }
-  if (need2 > 48 * 1024 && need2 > cur2) {
+  if (need1 > opt_in && need1 > cur1) {
+    e = cudaFuncSetAttribute(k_backtransform<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need1);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_backtransform<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need1);
+    if (e != cudaSuccess) return e;
+    cur1 = need1;
+  }
+  if (need2 > opt_in && need2 > cur2) {
     e = cudaFuncSetAttribute(k_tridiag, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need2);
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(k_invit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need2);
     if (e != cudaSuccess) return e;
     cur2 = need2;
   }
-  if (need3 > 48 * 1024 && need3 > cur3) {
+  if (need3 > opt_in && need3 > cur3) {
     e = cudaFuncSetAttribute(k_bisect, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need3);
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(k_tridiag_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need3);

@@ -234,7 +234,7 @@ __global__ void __launch_bounds__(kMixThreads) k_charges_mix(DevParams p, DevPla
       en[5] = g;
       en[0] = erep + eh0 + es2 + es3 + g;
       if (!isfinite(en[0])) w.status[m] |= GBXTB_MOL_NONFINITE;
-      w.phase[m] = kPhaseDone;
+      w.phase[m] = pl.pool ? kPhaseFinished : kPhaseDone;
     }
     return;
   }
@@ -367,32 +367,42 @@ __global__ void __launch_bounds__(kMixThreads) k_charges_mix(DevParams p, DevPla
   if (threadIdx.x == 0) w.nhist[m] = nst + 1;
 }
 
-// Count and list the molecules that still iterate (in index order).
-__global__ void k_count_active(DevPlan pl, Work w) {
-  __shared__ int s_base;
-  if (threadIdx.x == 0) s_base = 0;
+// Count and list (in index order) the molecules that still iterate, and
+// among them those whose next pass is FP64 with more than kClusterMinN AOs.
+__device__ __forceinline__ int block_compact(bool flag, int base, int32_t *list, int m, int *wsum) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int act = flag ? 1 : 0;
+  int incl = act;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) wsum[wid] = incl;
   __syncthreads();
+  int off = 0, tot = 0;
+  for (int k = 0; k < nw; ++k) {
+    if (k < wid) off += wsum[k];
+    tot += wsum[k];
+  }
+  if (act) list[base + off + incl - 1] = m;
+  __syncthreads();
+  return base + tot;
+}
+
+__global__ void k_count_active(DevPlan pl, Work w) {
+  __shared__ int wsum[32];
+  int base = 0, base64 = 0;
   for (int m0 = 0; m0 < pl.nmol; m0 += blockDim.x) {
     const int m = m0 + threadIdx.x;
-    const int act = (m < pl.nmol && w.phase[m] != kPhaseDone) ? 1 : 0;
-    // block-wide exclusive scan of act
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    int incl = act;
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += y;
-    }
-    __shared__ int wsum[32];
-    if (lane == 31) wsum[wid] = incl;
-    __syncthreads();
-    int off = 0;
-    for (int k = 0; k < wid; ++k) off += wsum[k];
-    if (act) w.active_list[s_base + off + incl - 1] = m;
-    __syncthreads();
-    if (threadIdx.x == blockDim.x - 1) s_base += off + incl;
-    __syncthreads();
+    const bool act = m < pl.nmol && (w.phase[m] == kPhaseIterate || w.phase[m] == kPhaseFinal);
+    const bool big64 = act && w.prec[m] != 0 && pl.mol[m].nao > kClusterMinN;
+    base = block_compact(act, base, w.active_list, m, wsum);
+    base64 = block_compact(big64, base64, w.big64_list, m, wsum);
   }
-  if (threadIdx.x == 0) w.active[0] = s_base;
+  if (threadIdx.x == 0) {
+    w.active[0] = base;
+    w.active[1] = base64;
+  }
 }
 
 __global__ void k_outputs(DevPlan pl, Work w, double *energy_out, double *charges_out) {

@@ -1,0 +1,284 @@
+"""Continuous batching of GFN1-xTB single points with forces.
+
+A ``Server`` keeps one slot pool (``gbxtb_pool_*`` in ``include/gbxtb.h``)
+per molecule-size class on the GPU.  Requests are queued on submission and
+admitted into a free slot of the smallest class that fits them, between any
+two SCF passes; every ``step`` runs one SCF pass for every molecule on the
+device (the pools of the size classes on their own CUDA streams, so their
+work overlaps), computes the forces of the molecules that converged, and
+hands their results back.  Converged molecules leave at once and their slots
+take the next requests, so requests that arrive while others are on the GPU
+join the running batch instead of waiting for it to drain.
+
+Slot counts follow a device-memory budget: a slot of capacity N AOs holds
+its molecule's SCF state (about 14 N^2 doubles).
+
+Per molecule the result is the single point of
+``dxtb_gb300.GFN1Calculator`` (the reference's ``get_energy`` /
+``get_forces``, ``calculators/types/energy.py:78-402``,
+``types/autograd.py:82-201``); the reference itself has no serving form.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+from collections import deque
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _lib, params
+from .calculator import DEFAULT_OPTS, _Context
+
+__all__ = ["Server", "Request", "size_class_capacity"]
+
+# (max atoms, share of the memory budget) of the default size classes
+DEFAULT_CLASSES = ((32, 0.15), (100, 0.25), (200, 0.3), (400, 0.3))
+
+
+def size_class_capacity(max_atoms: int) -> tuple[int, int]:
+    """Shells and AOs reserved for a slot of ``max_atoms`` atoms: enough for
+    molecules of elements with s and p valence shells (H-Ne and the heavier
+    main-group elements without d shells: two shells, at most four AOs per
+    atom); larger molecules go to a larger class."""
+    return 2 * max_atoms, 4 * max_atoms
+
+
+def slot_bytes(max_atoms: int) -> int:
+    nsh, nao = size_class_capacity(max_atoms)
+    # workspace: 8 + 5 matrices of nao^2 doubles, the shell-pair Coulomb
+    # matrix, mixer history and vectors
+    return 8 * (13 * nao * nao + nsh * nsh + 60 * nsh + 20 * nao) + 64 * max_atoms
+
+
+@dataclass
+class Request:
+    id: int
+    numbers: np.ndarray
+    positions: np.ndarray
+    charge: float = 0.0
+    spin: int | None = None
+    t_submit: float = 0.0
+    t_admit: float | None = None
+    t_done: float | None = None
+    energy: float | None = None
+    gradient: np.ndarray | None = None
+    charges: np.ndarray | None = None
+    status: int | None = None
+    iterations: int | None = None
+    size_class: int | None = None
+
+    @property
+    def latency(self) -> float | None:
+        return None if self.t_done is None else self.t_done - self.t_submit
+
+
+class _Pool:
+    """One size class: a ``gbxtb_pool`` and its stream."""
+
+    def __init__(self, ctx: _Context, opts: _lib.Options, max_atoms: int, nslots: int, device: int,
+                 priority: int = 0):
+        self.lib = _lib.load()
+        self.max_atoms = max_atoms
+        self.nslots = nslots
+        nsh, nao = size_class_capacity(max_atoms)
+        h = C.c_void_p()
+        nbytes = C.c_size_t()
+        with torch.cuda.device(device):
+            _lib.check(self.lib.gbxtb_pool_create(ctx.handle, C.byref(opts), nslots, max_atoms, nsh, nao,
+                                                  C.byref(h), C.byref(nbytes)))
+            # smaller size classes get higher stream priority: when SMs free
+            # up, their short passes go before the long passes of large
+            # molecules, which keeps the latency of small requests low
+            self.stream = torch.cuda.Stream(device, priority=priority)
+        self.handle = h
+        self.device_bytes = int(nbytes.value)
+        self.requests: dict[int, Request] = {}  # slot -> request
+        self._ended = np.zeros(nslots, dtype=np.int32)
+        self.launched = False
+
+    def free(self) -> int:
+        return int(self.lib.gbxtb_pool_free_slots(self.handle))
+
+    def admit(self, req: Request) -> bool:
+        num = np.ascontiguousarray(req.numbers, dtype=np.int32)
+        pos = np.ascontiguousarray(req.positions, dtype=np.float64)
+        slot = C.c_int32()
+        rc = self.lib.gbxtb_pool_admit(self.handle, len(num), _lib.ptr(num, C.c_int32), _lib.ptr(pos, C.c_double),
+                                       float(req.charge), -1 if req.spin is None else int(req.spin),
+                                       C.byref(slot))
+        if rc == -4:  # GBXTB_ERR_WORKSPACE: does not fit (or no free slot)
+            return False
+        _lib.check(rc)
+        self.requests[slot.value] = req
+        return True
+
+    def launch(self) -> None:
+        _lib.check(self.lib.gbxtb_pool_step_launch(self.handle, C.c_void_p(self.stream.cuda_stream)))
+        self.launched = True
+
+    def ready(self) -> bool:
+        rc = self.lib.gbxtb_pool_step_poll(self.handle)
+        if rc < 0:
+            _lib.check(rc)
+        return rc == 1
+
+    def finish(self) -> list[Request]:
+        n = C.c_int32()
+        it = C.c_int32()
+        _lib.check(self.lib.gbxtb_pool_step_finish(self.handle, _lib.ptr(self._ended, C.c_int32), C.byref(n),
+                                                   C.byref(it)))
+        self.launched = False
+        self.iterating = it.value
+        done = []
+        for k in range(n.value):
+            slot = int(self._ended[k])
+            req = self.requests.pop(slot)
+            nat = len(req.numbers)
+            e = np.zeros(1)
+            q = np.zeros(nat)
+            g = np.zeros((nat, 3))
+            st = C.c_int32()
+            its = C.c_int32()
+            _lib.check(self.lib.gbxtb_pool_result(self.handle, slot, _lib.ptr(e, C.c_double), _lib.ptr(q, C.c_double),
+                                                  _lib.ptr(g, C.c_double), C.byref(st), C.byref(its)))
+            req.energy, req.charges, req.gradient = float(e[0]), q, g
+            req.status, req.iterations = int(st.value), int(its.value)
+            done.append(req)
+        return done
+
+    @property
+    def busy(self) -> bool:
+        return bool(self.requests)
+
+    def __del__(self):
+        try:
+            if getattr(self, "handle", None) is not None and self.handle.value:
+                self.lib.gbxtb_pool_destroy(self.handle)
+        except Exception:  # pragma: no cover - interpreter shutdown
+            pass
+
+
+class Server:
+    """Continuous-batching GFN1 single points with forces on one GPU.
+
+    ``classes``: ``(max_atoms, nslots)`` pairs, or ``(max_atoms, share)``
+    pairs with ``share`` < 1 of a ``memory_gb`` device-memory budget.
+    ``opts``: calculator options (``dxtb_gb300.calculator.DEFAULT_OPTS``)."""
+
+    def __init__(self, classes=DEFAULT_CLASSES, opts: dict | None = None, memory_gb: float = 16.0,
+                 device: int | None = None, max_slots: int = 512):
+        if device is None:
+            device = torch.cuda.current_device()
+        self.device = device
+        o = dict(DEFAULT_OPTS)
+        o.update(opts or {})
+        excl = set(o.get("exclude", []))
+        if "disp" not in excl:
+            raise ValueError("D3 dispersion is not available; pass opts={'exclude': ['disp']}")
+        opt = _lib.Options()
+        opt.maxiter = int(o["maxiter"])
+        opt.fermi_maxiter = int(o["fermi_maxiter"])
+        opt.broyden_memory = int(o["broyden_memory"])
+        opt.want_forces = 1
+        opt.x_atol = float(o["x_atol"])
+        opt.x_atol_max = float(o["x_atol_max"])
+        opt.kt = float(o["fermi_etemp"]) * params.KELVIN2AU
+        opt.broyden_alpha = float(o["broyden_alpha"])
+        opt.profile = 0
+        opt.mixed_precision = 1 if o.get("mixed_precision", True) else 0
+        self.opts = o
+        ctx = _Context.get(device)
+        self.pools: list[_Pool] = []
+        for rank, (max_atoms, amount) in enumerate(sorted(classes)):
+            amount = float(amount)
+            if amount < 1:
+                nslots = int(amount * memory_gb * 1e9 // slot_bytes(max_atoms))
+            else:
+                nslots = int(amount)
+            nslots = max(1, min(max_slots, nslots))
+            # priority -1 (high) for the two smallest classes, 0 (normal) for the rest
+            self.pools.append(_Pool(ctx, opt, int(max_atoms), nslots, device, priority=-1 if rank <= 1 else 0))
+        self.queue: deque[Request] = deque()
+        self.completed: list[Request] = []
+        self._next_id = 0
+        self.steps = 0
+
+    @property
+    def device_bytes(self) -> int:
+        return sum(p.device_bytes for p in self.pools)
+
+    def submit(self, numbers, positions, charge: float = 0.0, spin: int | None = None,
+               t_submit: float | None = None) -> Request:
+        """Queue one single point (host arrays; positions in bohr)."""
+        num = np.asarray(numbers)
+        if len(num) > self.pools[-1].max_atoms:
+            raise ValueError(f"molecule with {len(num)} atoms exceeds the largest size class")
+        req = Request(self._next_id, num, np.asarray(positions, dtype=np.float64), float(charge), spin,
+                      time.perf_counter() if t_submit is None else t_submit)
+        self._next_id += 1
+        self.queue.append(req)
+        return req
+
+    def _admit(self) -> None:
+        waiting = deque()
+        while self.queue:
+            req = self.queue.popleft()
+            placed = False
+            for c, pool in enumerate(self.pools):
+                if len(req.numbers) <= pool.max_atoms and pool.free() > 0 and pool.admit(req):
+                    req.t_admit = time.perf_counter()
+                    req.size_class = c
+                    placed = True
+                    break
+            if not placed:
+                waiting.append(req)
+        self.queue = waiting
+
+    def step(self, wait: bool = True) -> list[Request]:
+        """Advance every pool at its own pace: collect the pools whose step
+        has completed, admit queued requests into free slots, and launch the
+        next step of every idle pool that holds molecules (the size classes
+        overlap on their streams; a pool of small molecules does not wait
+        for the slow passes of large ones).  Returns the requests that
+        completed.  ``wait``: block until at least one pool's step ends
+        when every busy pool is still running."""
+        done = []
+        while True:
+            for p in self.pools:
+                if p.launched and p.ready():
+                    done.extend(p.finish())
+            self._admit()
+            for p in self.pools:
+                if not p.launched and p.busy:
+                    p.launch()
+                    self.steps += 1
+            if done or not wait or not any(p.launched for p in self.pools):
+                break
+            time.sleep(5e-5)
+        now = time.perf_counter()
+        for r in done:
+            r.t_done = now
+        self.completed.extend(done)
+        return done
+
+    @property
+    def idle(self) -> bool:
+        return not self.queue and not any(p.busy or p.launched for p in self.pools)
+
+    def run_until_idle(self, max_steps: int = 100000) -> list[Request]:
+        out = []
+        for _ in range(max_steps):
+            if self.idle:
+                break
+            out.extend(self.step())
+        return out
+
+
+def latency_summary(requests) -> dict:
+    lat = np.array([r.latency for r in requests if r.latency is not None])
+    if lat.size == 0:
+        return {"p50_ms": None, "p99_ms": None}
+    return {"p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
+            "mean_ms": float(lat.mean() * 1e3)}

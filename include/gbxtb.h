@@ -159,6 +159,18 @@ GBXTB_API int gbxtb_singlepoint(gbxtb_plan *plan, const gbxtb_options *opts,
                       void *workspace_dev, size_t workspace_bytes,
                       void *stream);
 
+/* Autotune the launch shapes of the eigensolver kernels for this plan on
+ * real data: sets up the geometry of `positions_dev`, forms the first
+ * pass's FP32 Fock matrices, and times the candidates of (a) warps per CTA
+ * of the on-chip FP32 tridiagonalisation for each molecule-size class
+ * (8, 16, 32) and (b) threads per CTA of the eigenvalue search (64, 128,
+ * 256), keeping the fastest.  Later gbxtb_singlepoint calls use them.
+ * choice (nullable, 4 ints): the warps of the 3 size classes, then the
+ * threads.  No counterpart in the reference (which calls LAPACK/cuSOLVER). */
+GBXTB_API int gbxtb_plan_autotune(gbxtb_plan *plan, const gbxtb_options *opts,
+                                  const double *positions_dev, void *workspace_dev,
+                                  size_t workspace_bytes, void *stream, int32_t *choice);
+
 /* Per-molecule status bits and SCF iteration counts of the last
  * gbxtb_singlepoint on this plan (host arrays of nmol). Synchronises the
  * stream of that call. */
@@ -182,6 +194,59 @@ GBXTB_API int gbxtb_get_profile(gbxtb_plan *plan, double *ms, int64_t *launches,
  * potential of the reference (scf/base.py:701-727) is this value repeated
  * over the 2l+1 orbitals of each shell.  Synchronises that call's stream. */
 GBXTB_API int gbxtb_get_shell_potential(gbxtb_plan *plan, double *potential);
+
+/* ---------------------------------------------------------------------------
+ * Slot pool: continuous batching of single points with forces (serving).
+ * A pool holds nslots molecules of up to cap_atoms atoms, cap_shells shells
+ * and cap_aos AOs each, with their SCF state resident on the device.
+ * Requests are admitted into free slots at any time (gbxtb_pool_admit); each
+ * step (gbxtb_pool_step_launch + gbxtb_pool_step_finish) sets up the newly
+ * admitted molecules, runs one SCF pass for every molecule in the pool, and
+ * computes the forces of those that converged; their slots report as ended,
+ * and gbxtb_pool_result copies a result out and frees its slot for the next
+ * request.  Several pools (size classes) can step on different streams at
+ * once: launch them all, then finish them.
+ * Per molecule this is the reference's single point with autograd forces
+ * (calculators/types/energy.py:78-402, types/autograd.py:82-201); the
+ * reference has no serving form (it is a library called once per input).
+ * opts->want_forces is implied; opts->profile must be 0.
+ * ------------------------------------------------------------------------- */
+typedef struct gbxtb_pool gbxtb_pool;
+
+GBXTB_API int gbxtb_pool_create(gbxtb_ctx *ctx, const gbxtb_options *opts, int32_t nslots,
+                                int32_t cap_atoms, int32_t cap_shells, int32_t cap_aos,
+                                gbxtb_pool **out, size_t *device_bytes);
+GBXTB_API void gbxtb_pool_destroy(gbxtb_pool *pool);
+
+/* Free slots of the pool (or a negative error code). */
+GBXTB_API int gbxtb_pool_free_slots(const gbxtb_pool *pool);
+
+/* Admit one molecule (host arrays: numbers[natoms], positions[natoms][3] in
+ * bohr; uhf < 0: from the electron parity).  *slot receives its slot; it
+ * starts at the next step.  GBXTB_ERR_WORKSPACE: no free slot, or the
+ * molecule exceeds the slot capacity. */
+GBXTB_API int gbxtb_pool_admit(gbxtb_pool *pool, int32_t natoms, const int32_t *numbers,
+                               const double *positions, double charge, int32_t uhf, int32_t *slot);
+
+/* Enqueue one step on `stream` (a cudaStream_t). */
+GBXTB_API int gbxtb_pool_step_launch(gbxtb_pool *pool, void *stream);
+
+/* 1 if the launched step has completed (or none is in flight), 0 if it is
+ * still running, negative on error.  Lets a host drive several pools, each
+ * at its own pace, without blocking on the slowest. */
+GBXTB_API int gbxtb_pool_step_poll(gbxtb_pool *pool);
+
+/* Wait for the step; ended[0..*nended) receive the slots whose molecule
+ * ended in it (host array of nslots; nullable), *iterating the molecules
+ * still iterating (nullable). */
+GBXTB_API int gbxtb_pool_step_finish(gbxtb_pool *pool, int32_t *ended, int32_t *nended,
+                                     int32_t *iterating);
+
+/* Result of an ended slot (host arrays: energy[1], charges[natoms],
+ * gradient[natoms][3] = dE/dR, status[1], iterations[1]; each nullable);
+ * frees the slot. */
+GBXTB_API int gbxtb_pool_result(gbxtb_pool *pool, int32_t slot, double *energy, double *charges,
+                                double *gradient, int32_t *status, int32_t *iterations);
 
 /* Device scratch compiled into the library for gbxtb_singlepoint_noalloc. */
 #define GBXTB_NOALLOC_SCRATCH_BYTES ((size_t)32 * 1024 * 1024)

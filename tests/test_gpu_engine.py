@@ -214,3 +214,17 @@ def test_mixed_precision_same_fixed_point():
     off = np.concatenate([[0], np.cumsum([len(m[0]) for m in mols])])
     for k in same:
         assert np.abs(g64[off[k]:off[k + 1]] - g32[off[k]:off[k + 1]]).max() < 1e-8
+
+
+def test_large_molecule_against_oracle():
+    """A 300-atom molecule (~900 AOs): the block-wise Cholesky over the whole
+    GPU, the global-memory lead-in of the on-chip FP32 tridiagonalisation
+    and the cluster FP64 passes, against the oracle."""
+    num, pos = molgen.grow(300, 4253)
+    calc = calc_for(num)
+    res = calc.singlepoint(torch.tensor(pos, device="cuda"), forces=True)
+    r = go.singlepoint(num, pos, mixer="broyden")
+    assert res.status[0] == 0 and r.converged
+    if same_state(res.energy.item(), r.energy):
+        assert abs(res.energy.item() - r.energy) < E_TOL
+        assert np.abs(-res.gradient.cpu().numpy() - r.forces).max() < F_TOL
