@@ -450,9 +450,9 @@ int enqueue_setup(gbxtb_plan *plan, const Work &w, const gbxtb_options &o, const
 
 namespace {
 // Enqueue one SCF pass on stream s: lists of iterating molecules at most
-// `active` long (tail shapes), large FP64 passes at most `big64`.  Returns
+// `active` long (tail shapes), cluster passes at most `nclus`.  Returns
 // the number of kernel launches; times kernel classes when pf is given.
-int enqueue_pass(gbxtb_plan *plan, const Work &w, const gbxtb_options &o, bool tail, int active, int big64,
+int enqueue_pass(gbxtb_plan *plan, const Work &w, const gbxtb_options &o, bool tail, int active, int nclus,
                  cudaStream_t s, Prof *pf) {
   const DevPlan &pl = plan->pl;
   const DevParams &p = plan->ctx->p;
@@ -469,14 +469,11 @@ int enqueue_pass(gbxtb_plan *plan, const Work &w, const gbxtb_options &o, bool t
   if (opts->mixed_precision) launch_tridiag_smem(pl, w, s);
   int ntrd = opts->mixed_precision ? plan->smem_launches : 0;
   if (tail) {
-    launch_tridiag_cluster(pl, w, w.active_list, active, plan->maxn, s);
-    ntrd += 1;
+    ntrd += launch_tridiag_cluster(pl, w, w.active_list, active, plan->maxn, s);
   } else {
-    // large FP64 passes on 8-SM clusters, the rest one CTA per molecule
-    if (big64 > 0) {
-      launch_tridiag_cluster(pl, w, w.big64_list, big64, plan->maxn, s);
-      ntrd += 1;
-    }
+    // large FP64 passes and FP32 passes too large for shared memory on 8-SM
+    // clusters, the rest one CTA per molecule
+    if (nclus > 0) ntrd += launch_tridiag_cluster(pl, w, w.cluster_list, nclus, plan->maxn, s);
     launch_tridiag(pl, w, plan->maxn, s);
     ntrd += 1;
   }
@@ -544,11 +541,11 @@ int gbxtb_singlepoint(gbxtb_plan *plan, const gbxtb_options *opts, const double 
   // SCF: maxiter mixing iterations + the first evaluation + the final pass
   const int max_loops = opts->maxiter + 3;
   int active = pl.nmol;  // molecules iterating (known after each pass)
-  int big64 = 0;         // of those, FP64 passes on a cluster
+  int nclus = 0;         // of those, passes that tridiagonalise on a cluster
   launch_count_active(pl, w, s);
   CK(cudaMemcpyAsync(plan->h_active, w.active, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
-  big64 = plan->h_active[1];
+  nclus = plan->h_active[1];
   plan->total_launches += 1;
   // the passes: replayed as a CUDA graph of one pass (one graph launch and
   // one 8-byte copy per pass), or launched one by one with per-class timing
@@ -601,14 +598,14 @@ int gbxtb_singlepoint(gbxtb_plan *plan, const gbxtb_options *opts, const double 
       CK(cudaGraphLaunch(plan->pass_graph[tail ? 1 : 0], s));
       plan->total_launches += plan->pass_graph_launches[tail ? 1 : 0];
     } else {
-      enqueue_pass(plan, w, *opts, tail, active, big64, s, &pf);
+      enqueue_pass(plan, w, *opts, tail, active, nclus, s, &pf);
       CK(cudaMemcpyAsync(plan->h_active, w.active, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     }
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(s));
     pf.harvest();
     active = plan->h_active[0];
-    big64 = plan->h_active[1];
+    nclus = plan->h_active[1];
     if (active == 0) break;
   }
   launch_energies(p, pl, w, opts->kt, energy_dev, charges_dev, s);

@@ -14,8 +14,8 @@ void launch_gemm(const DevPlan &pl, const Work &w, const int64_t *tile0, int64_t
 void launch_tridiag(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s);
 void launch_lowp_copies(const DevPlan &pl, const Work &w, cudaStream_t s);
 void launch_tridiag_smem(const DevPlan &pl, const Work &w, cudaStream_t s);
-void launch_tridiag_cluster(const DevPlan &pl, const Work &w, const int32_t *mol_list, int count,
-                            int maxn, cudaStream_t s);
+int launch_tridiag_cluster(const DevPlan &pl, const Work &w, const int32_t *mol_list, int count, int maxn,
+                           cudaStream_t s);
 void launch_bisect(const DevPlan &pl, const Work &w, int maxn, double kt, const int32_t *mol_list, int count,
                    int threads, cudaStream_t s);
 void launch_invit(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s);
@@ -83,7 +83,7 @@ struct gbxtb_plan {
   int32_t *h_active = nullptr;  // pinned
   int num_sms = 0;
   int smem_launches = 0;  // size classes with molecules (k_tridiag_smem launches per pass)
-  int nbig = 0;           // molecules with more than kClusterMinN AOs
+  int nbig = 0;           // molecules with more than kClusterMinN AOs (cluster passes at most)
   // CUDA graphs of one SCF pass ([0]: launch shapes over all molecules, [1]:
   // the tail shapes), with the workspace and options they were captured for
   cudaGraphExec_t pass_graph[2] = {nullptr, nullptr};
@@ -133,7 +133,7 @@ inline Layout make_layout(const DevPlan &pl) {
   L.add(d * pl.nmol);                                       // best32
   L.add(i4 * 4);                                            // active
   L.add(i4 * pl.nmol);                                      // active_list
-  L.add(i4 * pl.nmol);                                      // big64_list
+  L.add(i4 * pl.nmol);                                      // cluster_list
   return L;
 }
 
@@ -159,7 +159,7 @@ inline Work make_work(const DevPlan &pl, void *base) {
   w.efermi = D(); w.energy = D(); w.resid = D(); w.best32 = D();
   w.active = I();
   w.active_list = I();
-  w.big64_list = I();
+  w.cluster_list = I();
   return w;
 }
 

@@ -38,6 +38,16 @@ constexpr int kCholBlockMinN = 192;
 // FP64 passes of molecules with more AOs than this tridiagonalise on an
 // 8-SM cluster (the FP64 pipe of one SM needs ~N^3 / 2 clocks)
 constexpr int kClusterMinN = 128;
+// Cluster passes of molecules with more AOs than this use the blocked
+// (panel) cluster tridiagonalisation; smaller ones the column-by-column one.
+constexpr int kClusterBlockedMinN = 400;
+
+// Passes that tridiagonalise on an 8-SM cluster in every pass (not only in
+// the tail of a batch): FP64 passes above kClusterMinN AOs and FP32 passes
+// too large for the shared-memory kernel.
+__host__ __device__ __forceinline__ bool cluster_pass(int prec, int nao) {
+  return prec ? nao > kClusterMinN : nao > kSmemTridiagMaxN;
+}
 
 // molecule phases of the SCF state machine
 constexpr int kPhaseIterate = 0;  // mixing iterations
@@ -114,7 +124,7 @@ struct Work {
   double *resid;    // [nmol][2]: L2, max norm of the last potential change
   int32_t *active;  // [2]: molecules not yet done; of those, FP64 passes with more than kClusterMinN AOs
   int32_t *active_list;  // [nmol]: indices of the molecules not yet done
-  int32_t *big64_list;   // [nmol]: indices of the FP64 passes with more than kClusterMinN AOs
+  int32_t *cluster_list;  // [nmol]: molecules whose next pass tridiagonalises on a cluster (cluster_pass)
 };
 
 // ---------------------------------------------------------------------------
@@ -205,7 +215,7 @@ __device__ __forceinline__ bool mol_running(const Work &w, int m) {
 // be sized by an upper bound of that length).
 __device__ __forceinline__ int list_mol(const Work &w, const int32_t *list, int idx) {
   if (list == w.active_list && idx >= w.active[0]) return -1;
-  if (list == w.big64_list && idx >= w.active[1]) return -1;
+  if (list == w.cluster_list && idx >= w.active[1]) return -1;
   return list[idx];
 }
 

@@ -450,8 +450,9 @@ __global__ void __launch_bounds__(kTrdThreads) k_tridiag(DevPlan pl, Work w) {
   const int m = blockIdx.x;
   if (w.phase[m] == kPhaseDone) return;
   const MolDesc md = pl.mol[m];
-  // FP32 passes that fit run in k_tridiag_smem, large FP64 passes on a cluster
-  if (w.prec[m] == 0 ? md.nao <= kSmemTridiagMaxN : md.nao > kClusterMinN) return;
+  // FP32 passes run in k_tridiag_smem or (too large for shared memory) on a
+  // cluster, like the FP64 passes of more than kClusterMinN AOs
+  if (w.prec[m] == 0 || cluster_pass(w.prec[m], md.nao)) return;
   extern __shared__ double sm[];
   __shared__ double red[32];
   if (w.prec[m])
@@ -714,8 +715,9 @@ __global__ void __launch_bounds__(NW * 32) k_tridiag_smem(DevPlan pl, Work w, co
 
 // ---------------------------------------------------------------------------
 // Householder tridiagonalisation on a thread-block cluster (8 SMs per
-// molecule) for latency: when few molecules are still iterating, one SM per
-// molecule leaves the GPU idle.  Rows are owned cyclically (row i by CTA
+// molecule), column by column, for molecules up to kClusterBlockedMinN AOs:
+// FP64 passes above kClusterMinN AOs, and every pass in the tail of a batch,
+// when one SM per molecule would leave the GPU idle.  Rows are owned cyclically (row i by CTA
 // i mod 8); every CTA rebuilds the reflector from the column in L2, forms
 // p = tau A v and the rank-2 update for its own rows, and the two global
 // quantities of a step (p.v and the vector w) are exchanged through
@@ -732,7 +734,7 @@ __device__ __forceinline__ T ld_cg(const T *p) {
 }
 
 template <typename T>
-__device__ __forceinline__ void tridiag_cluster_body(cg::cluster_group &cluster, const MolDesc &md,
+__device__ __forceinline__ void tridiag_cluster_unblocked(cg::cluster_group &cluster, const MolDesc &md,
                                                      const Work &w, T *sm, T *red, T *kpart) {
   const int rank = (int)cluster.block_rank();
   const int n = md.nao;
@@ -832,15 +834,313 @@ __global__ void __cluster_dims__(kClusterSize, 1, 1) __launch_bounds__(kTrdClThr
   __shared__ double red[32];
   __shared__ double kpart;
   // uniform over the cluster; FP32 passes of molecules that fit in shared
-  // memory run in k_tridiag_smem
-  const bool done = (w.phase[m] == kPhaseDone) || (w.prec[m] == 0 && md.nao <= kSmemTridiagMaxN);
+  // memory run in k_tridiag_smem, molecules above kClusterBlockedMinN AOs in
+  // k_tridiag_cluster_blocked
+  const bool done = (w.phase[m] == kPhaseDone) || (w.prec[m] == 0 && md.nao <= kSmemTridiagMaxN) ||
+                    md.nao > kClusterBlockedMinN;
   if (!done) {
     if (w.prec[m])
-      tridiag_cluster_body<double>(cluster, md, w, sm, red, &kpart);
+      tridiag_cluster_unblocked<double>(cluster, md, w, sm, red, &kpart);
     else
-      tridiag_cluster_body<float>(cluster, md, w, reinterpret_cast<float *>(sm),
-                                  reinterpret_cast<float *>(red), reinterpret_cast<float *>(&kpart));
+      tridiag_cluster_unblocked<float>(cluster, md, w, reinterpret_cast<float *>(sm),
+                                       reinterpret_cast<float *>(red), reinterpret_cast<float *>(&kpart));
   }
+  cluster.sync();
+}
+
+// ---------------------------------------------------------------------------
+// Blocked Householder tridiagonalisation on a thread-block cluster (8 SMs
+// per molecule) for molecules above kClusterBlockedMinN AOs.
+//
+// Rows are owned cyclically (row i by CTA i mod 8).  Columns are reduced in
+// panels of kPanel (LAPACK's dlatrd/dsytrd split): within a panel the
+// trailing matrix is left as it was at the panel start, and column c's
+// reflector and its vector w come from it plus the panel's earlier pairs
+// (v_l, w_l):
+//   a   = A[:, c] - sum_l (v_l w_l[c] + w_l v_l[c])
+//   p   = tau (A22 v - V (W^T v) - W (V^T v)),   w = p - tau/2 (p.v) v
+// and the rank-2 updates of the panel are applied to the trailing matrix at
+// its end in one pass (A22 -= V W^T + W V^T).  The matrix is therefore read
+// once per column (A22 v) and read and written once per panel, instead of
+// read twice and written once per column.
+//
+// Per column two cluster barriers: after the own rows' corrected column
+// entries are published (every CTA gathers the whole column from
+// distributed shared memory and builds the reflector), and after the
+// partial sums of A22 v, V^T v, W^T v are published.  The w of the next
+// row (c + 1), which the next column's correction needs before any
+// barrier, is computed identically by every CTA.
+//
+// Storage: v of column c goes to row c right of the diagonal (the
+// back-transformation reads it there); the panel's w vectors go to the
+// eigenvector matrix Z, free until the inverse iteration, as W[l][i]
+// (row-major, l < kPanel).  Same outputs d, e, tau as k_tridiag.
+// ---------------------------------------------------------------------------
+constexpr int kTrdBlkThreads = 512;
+constexpr int kPanel = 32;    // columns per panel
+constexpr int kUpdRows = 64;  // own rows per trailing-update tile
+constexpr int kUpdCols = 64;  // columns per trailing-update tile
+
+// dynamic shared memory of k_tridiag_cluster_blocked for molecules up to maxn AOs
+// (laid out in 8-byte slots for both precisions)
+inline size_t tridiag_cluster_smem_bytes(int maxn) {
+  const size_t slots = 2 * (size_t)maxn + (size_t)maxn / kClusterSize + 2 + 6 * kPanel + 4 +
+                       2 * (size_t)kPanel * (kUpdRows + kUpdCols);
+  return sizeof(double) * slots;
+}
+
+// row . v over m1 entries, lanes strided, four loads in flight per lane;
+// the warp sum is returned in every lane
+template <typename T, bool CG>
+__device__ __forceinline__ T row_dot(const T *row, const T *v, int m1, int lane) {
+  T a0 = T(0), a1 = T(0), a2 = T(0), a3 = T(0);
+  int t = lane;
+  for (; t + 96 < m1; t += 128) {
+    a0 += (CG ? ld_cg(row + t) : row[t]) * v[t];
+    a1 += (CG ? ld_cg(row + t + 32) : row[t + 32]) * v[t + 32];
+    a2 += (CG ? ld_cg(row + t + 64) : row[t + 64]) * v[t + 64];
+    a3 += (CG ? ld_cg(row + t + 96) : row[t + 96]) * v[t + 96];
+  }
+  for (; t < m1; t += 32) a0 += (CG ? ld_cg(row + t) : row[t]) * v[t];
+  return warp_sum((a0 + a1) + (a2 + a3));
+}
+
+template <typename T>
+__device__ __forceinline__ void tridiag_cluster_blocked(cg::cluster_group &cluster, const MolDesc &md,
+                                                        const Work &w, T *sm, T *red) {
+  const int rank = (int)cluster.block_rank();
+  const int n = md.nao;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  constexpr int NW = kTrdBlkThreads / 32;
+  T *A = mat_view<T>(w.A, md.mat0);
+  T *W = mat_view<T>(w.Z, md.mat0);  // W[l * n + i], l < kPanel
+  double *d = w.d + md.ao0, *e = w.e + md.ao0, *tau = w.tau + md.ao0;
+  // shared memory (8-byte slots, see tridiag_cluster_smem_bytes)
+  T *vs = sm;                                              // [n] reflector of the current column
+  T *xs = sm + n;                                          // [n] own corrected column entries (DSMEM)
+  T *ys = sm + 2 * n;                                      // [n / 8 + 1] own rows' A22 v
+  T *part = ys + n / kClusterSize + 2;                     // [2 kPanel + 2] own partial sums (DSMEM)
+  T *x12 = part + 2 * kPanel + 2;                          // [2 kPanel] totals of W^T v, V^T v
+  T *coef = x12 + 2 * kPanel;                              // [2 kPanel + 2] row c's W, V entries; scalars
+  T *tile = coef + 2 * kPanel + 2;                         // trailing-update tiles
+  constexpr int kNorm = 2 * kPanel, kVav = 2 * kPanel + 1;
+  T wnext = T(0);  // w of row c + 1 (identical in every CTA)
+  // own rows are i = rank + 8 g
+  auto first_own = [&](int lo) {  // smallest own row >= lo
+    return lo + ((rank - lo) % kClusterSize + kClusterSize) % kClusterSize;
+  };
+  for (int p0 = 0; p0 + 2 < n; p0 += kPanel) {
+    const int pw = min(kPanel, n - 2 - p0);
+    for (int jj = 0; jj < pw; ++jj) {
+      const int c = p0 + jj;
+      const int m1 = n - c - 1;
+      // --- A: corrected entries of column c in the own rows i > c ---------
+      // coefficients of row c: W[l][c], V[l][c] = A[p0 + l][c]; the previous
+      // column's pair is not yet in global memory for other CTAs: its w(c)
+      // is wnext, its v(c) = 1, and its v in the own rows is still in vs
+      if (tid < jj) {
+        coef[tid] = (tid == jj - 1) ? wnext : ld_cg(W + (int64_t)tid * n + c);
+        coef[kPanel + tid] = (tid == jj - 1) ? T(1) : ld_cg(A + (int64_t)(p0 + tid) * n + c);
+      }
+      __syncthreads();
+      T nrm = T(0);
+      for (int i = first_own(c + 1) + kClusterSize * tid; i < n; i += kClusterSize * kTrdBlkThreads) {
+        T x = A[(int64_t)i * n + c];
+        for (int l = 0; l + 1 < jj; ++l)
+          x -= ld_cg(A + (int64_t)(p0 + l) * n + i) * coef[l] + W[(int64_t)l * n + i] * coef[kPanel + l];
+        if (jj > 0) x -= vs[i - c] * coef[jj - 1] + W[(int64_t)(jj - 1) * n + i] * coef[kPanel + jj - 1];
+        xs[i - c - 1] = x;
+        if (i > c + 1) nrm += x * x;
+      }
+      nrm = block_sum(nrm, red);
+      if (tid == 0) part[kNorm] = nrm;
+      cluster.sync();
+      // --- B: reflector, A22 v and the partial sums -------------------------
+      T xn2 = T(0);
+      for (int r = 0; r < kClusterSize; ++r) xn2 += *cluster.map_shared_rank(part + kNorm, r);
+      for (int t = tid; t < m1; t += kTrdBlkThreads)
+        vs[t] = *cluster.map_shared_rank(xs + t, (c + 1 + t) % kClusterSize);
+      __syncthreads();
+      const T alpha = vs[0];
+      T tk = T(0), scale = T(0), beta = alpha;
+      if (xn2 != T(0)) {
+        beta = -copysign(sqrt(alpha * alpha + xn2), alpha);
+        tk = (beta - alpha) / beta;
+        scale = T(1) / (alpha - beta);
+      }
+      if (rank == 0 && tid == 0) {
+        T dc = ld_cg(A + (int64_t)c * n + c);
+        for (int l = 0; l < jj; ++l) dc -= T(2) * coef[l] * coef[kPanel + l];
+        d[c] = dc;
+        e[c] = beta;
+        tau[c] = tk;
+      }
+      __syncthreads();  // every thread has read alpha
+      for (int t = tid; t < m1; t += kTrdBlkThreads) vs[t] = (t == 0) ? T(1) : vs[t] * scale;
+      __syncthreads();
+      // y = A22 v for the own rows, one warp per row, and for row c + 1 in
+      // every CTA (by warp 0, in the same order everywhere)
+      T s1 = T(0), s2 = T(0), svav = T(0);  // lane l: partial W^T v, V^T v
+      {
+        const int own0 = first_own(c + 1);
+        for (int i = own0 + kClusterSize * wid; i < n; i += kClusterSize * NW) {
+          if (i == c + 1) continue;  // taken below
+          const T acc = row_dot<T, false>(A + (int64_t)i * n + (c + 1), vs, m1, lane);
+          const T vi = vs[i - c - 1];
+          if (lane == 0) ys[i / kClusterSize] = acc;
+          svav += vi * acc;  // identical in every lane
+          if (lane < jj) {
+            s1 += W[(int64_t)lane * n + i] * vi;
+            s2 += ld_cg(A + (int64_t)(p0 + lane) * n + i) * vi;
+          }
+        }
+      }
+      if (wid == 0) {
+        const T acc = row_dot<T, true>(A + (int64_t)(c + 1) * n + (c + 1), vs, m1, lane);
+        if (lane == 0) coef[2 * kPanel] = acc;  // y(c + 1)
+        if ((c + 1) % kClusterSize == rank) {
+          svav += acc;  // v(c + 1) = 1
+          if (lane < jj) {
+            s1 += ld_cg(W + (int64_t)lane * n + c + 1);
+            s2 += ld_cg(A + (int64_t)(p0 + lane) * n + c + 1);
+          }
+        }
+      }
+      // reduce the per-lane partials over the warps: tile[wid][0..2 kPanel]
+      {
+        T *pw_part = tile + wid * (2 * kPanel + 1);
+        pw_part[lane] = s1;
+        pw_part[kPanel + lane] = s2;
+        if (lane == 0) pw_part[2 * kPanel] = svav;
+        __syncthreads();
+        if (tid < 2 * kPanel + 1) {
+          T s = T(0);
+          for (int q = 0; q < NW; ++q) s += tile[q * (2 * kPanel + 1) + tid];
+          if (tid < 2 * kPanel) part[tid] = s;
+          else part[kVav] = s;
+        }
+      }
+      cluster.sync();
+      // --- C: w for the own rows and for row c + 1 ---------------------------
+      if (tid <= 2 * kPanel) {
+        const int slot = (tid < 2 * kPanel) ? tid : kVav;
+        T s = T(0);
+        for (int r = 0; r < kClusterSize; ++r) s += *cluster.map_shared_rank(part + slot, r);
+        if (tid < 2 * kPanel) x12[tid] = s;
+        else coef[2 * kPanel + 1] = s;  // v^T A22 v
+      }
+      __syncthreads();
+      T x1x2 = T(0);
+      for (int l = 0; l < jj; ++l) x1x2 += x12[l] * x12[kPanel + l];
+      const T K = tk * (coef[2 * kPanel + 1] - T(2) * x1x2);
+      const T half = T(0.5) * tk * K;
+      // own rows: w_i = tk (y_i - sum_l V[l][i] x1_l - W[l][i] x2_l) - half v_i
+      for (int i = first_own(c + 2) + kClusterSize * wid; i < n; i += kClusterSize * NW) {
+        T corr = T(0);
+        if (lane < jj)
+          corr = ld_cg(A + (int64_t)(p0 + lane) * n + i) * x12[lane] + W[(int64_t)lane * n + i] * x12[kPanel + lane];
+        corr = warp_sum(corr);
+        if (lane == 0) W[(int64_t)jj * n + i] = tk * (ys[i / kClusterSize] - corr) - half * vs[i - c - 1];
+      }
+      // row c + 1, in every CTA (warp 0, the same order everywhere)
+      if (wid == 0) {
+        T corr = T(0);
+        if (lane < jj)
+          corr = ld_cg(A + (int64_t)(p0 + lane) * n + c + 1) * x12[lane] +
+                 ld_cg(W + (int64_t)lane * n + c + 1) * x12[kPanel + lane];
+        corr = warp_sum(corr);
+        const T wn = tk * (coef[2 * kPanel] - corr) - half;  // v(c + 1) = 1
+        if (lane == 0) {
+          coef[2 * kPanel] = wn;
+          if ((c + 1) % kClusterSize == rank) W[(int64_t)jj * n + c + 1] = wn;
+        }
+      }
+      // v into row c (read by other CTAs only after the next barrier)
+      if (rank == 0)
+        for (int t = tid; t < m1; t += kTrdBlkThreads) A[(int64_t)c * n + c + 1 + t] = vs[t];
+      __syncthreads();
+      wnext = coef[2 * kPanel];
+    }
+    // --- trailing update of the own rows i >= pe, columns j >= pe -----------
+    cluster.sync();  // every w and v of the panel is visible
+    const int pe = p0 + pw;
+    T *Vr = tile, *Wr = tile + kPanel * kUpdRows;  // [l][q]
+    T *Vc = Wr + kPanel * kUpdRows, *Wc = Vc + kPanel * kUpdCols;  // [l][jc]
+    const int ty = tid / 16, tx = tid % 16;  // 2 rows x 4 columns per thread
+    for (int rb = first_own(pe); rb < n; rb += kClusterSize * kUpdRows) {
+      for (int k = tid; k < pw * kUpdRows; k += kTrdBlkThreads) {
+        const int l = k / kUpdRows, q = k % kUpdRows;
+        const int i = rb + kClusterSize * q;
+        Vr[k] = (i < n) ? ld_cg(A + (int64_t)(p0 + l) * n + i) : T(0);
+        Wr[k] = (i < n) ? ld_cg(W + (int64_t)l * n + i) : T(0);
+      }
+      for (int cb = pe; cb < n; cb += kUpdCols) {
+        __syncthreads();
+        for (int k = tid; k < pw * kUpdCols; k += kTrdBlkThreads) {
+          const int l = k / kUpdCols, jc = k % kUpdCols;
+          const int j = cb + jc;
+          Vc[k] = (j < n) ? ld_cg(A + (int64_t)(p0 + l) * n + j) : T(0);
+          Wc[k] = (j < n) ? ld_cg(W + (int64_t)l * n + j) : T(0);
+        }
+        __syncthreads();
+        T acc[2][4] = {};
+        for (int l = 0; l < pw; ++l) {
+          T vr[2], wr[2], vc[4], wc[4];
+#pragma unroll
+          for (int a = 0; a < 2; ++a) {
+            vr[a] = Vr[l * kUpdRows + 2 * ty + a];
+            wr[a] = Wr[l * kUpdRows + 2 * ty + a];
+          }
+#pragma unroll
+          for (int b = 0; b < 4; ++b) {
+            vc[b] = Vc[l * kUpdCols + 4 * tx + b];
+            wc[b] = Wc[l * kUpdCols + 4 * tx + b];
+          }
+#pragma unroll
+          for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) acc[a][b] += vr[a] * wc[b] + wr[a] * vc[b];
+        }
+#pragma unroll
+        for (int a = 0; a < 2; ++a) {
+          const int i = rb + kClusterSize * (2 * ty + a);
+          if (i >= n) continue;
+#pragma unroll
+          for (int b = 0; b < 4; ++b) {
+            const int j = cb + 4 * tx + b;
+            if (j < n) A[(int64_t)i * n + j] -= acc[a][b];
+          }
+        }
+      }
+      __syncthreads();
+    }
+    cluster.sync();  // updated rows visible before the next panel
+  }
+  if (rank == 0 && tid == 0) {
+    if (n >= 2) {
+      d[n - 2] = ld_cg(A + (int64_t)(n - 2) * n + (n - 2));
+      d[n - 1] = ld_cg(A + (int64_t)(n - 1) * n + (n - 1));
+      e[n - 2] = ld_cg(A + (int64_t)(n - 1) * n + (n - 2));
+    } else {
+      d[0] = ld_cg(A);
+    }
+  }
+}
+
+__global__ void __cluster_dims__(kClusterSize, 1, 1) __launch_bounds__(kTrdBlkThreads, 1)
+    k_tridiag_cluster_blocked(DevPlan pl, Work w, const int32_t *mol_list) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int m = list_mol(w, mol_list, blockIdx.x / kClusterSize);
+  if (m < 0) return;  // the whole cluster
+  const MolDesc md = pl.mol[m];
+  extern __shared__ double sm[];
+  __shared__ double red[32];
+  // uniform over the cluster; smaller molecules run in k_tridiag_cluster
+  if (w.phase[m] == kPhaseDone || md.nao <= kClusterBlockedMinN) return;
+  if (w.prec[m])
+    tridiag_cluster_blocked<double>(cluster, md, w, sm, red);
+  else
+    tridiag_cluster_blocked<float>(cluster, md, w, reinterpret_cast<float *>(sm), reinterpret_cast<float *>(red));
   cluster.sync();
 }
 
@@ -1485,11 +1785,16 @@ void launch_tridiag_smem(const DevPlan &pl, const Work &w, cudaStream_t s) {
 
 
 // Cluster tridiagonalisation for the molecules listed in mol_list (device).
-void launch_tridiag_cluster(const DevPlan &pl, const Work &w, const int32_t *mol_list, int count,
-                            int maxn, cudaStream_t s) {
-  if (count <= 0) return;
-  const size_t smem = sizeof(double) * 3 * (size_t)maxn;
+// Returns the number of launches.
+int launch_tridiag_cluster(const DevPlan &pl, const Work &w, const int32_t *mol_list, int count, int maxn,
+                           cudaStream_t s) {
+  if (count <= 0) return 0;
+  const size_t smem = sizeof(double) * 3 * (size_t)min(maxn, kClusterBlockedMinN);
   k_tridiag_cluster<<<count * kClusterSize, kTrdClThreads, smem, s>>>(pl, w, mol_list);
+  if (maxn <= kClusterBlockedMinN) return 1;
+  k_tridiag_cluster_blocked<<<count * kClusterSize, kTrdBlkThreads, tridiag_cluster_smem_bytes(maxn), s>>>(
+      pl, w, mol_list);
+  return 2;
 }
 
 // All molecules (mol_list null, count = nmol) with 256 threads per block,
@@ -1543,13 +1848,14 @@ void launch_backtransform(const DevPlan &pl, const Work &w, int maxn, const int3
 // wide, and plans created earlier keep launching, so it only ever grows.
 cudaError_t set_linalg_smem_limits(int maxn) {
   static std::mutex mu;
-  static size_t cur_smem = 0, cur1 = 0, cur2 = 0, cur3 = 0;
+  static size_t cur_smem = 0, cur1 = 0, cur2 = 0, cur3 = 0, cur_c = 0;
   std::lock_guard<std::mutex> lock(mu);
   // every warp count of k_tridiag_smem may serve any size class (autotuning)
   const size_t need_s = tridiag_smem_bytes(maxn < kSmemTridiagMaxN ? maxn : kSmemTridiagMaxN, 32);
   const size_t need1 = sizeof(double) * (size_t)maxn;
   const size_t need2 = sizeof(double) * 2 * (size_t)maxn;
   const size_t need3 = sizeof(double) * 3 * (size_t)maxn;
+  const size_t need_c = tridiag_cluster_smem_bytes(maxn);
   // above 48 KB of dynamic plus static shared memory a kernel needs the
   // attribute; the kernels' static arrays take at most 4 KB
   const size_t opt_in = 44 * 1024;
@@ -1580,9 +1886,12 @@ cudaError_t set_linalg_smem_limits(int maxn) {
   if (need3 > opt_in && need3 > cur3) {
     e = cudaFuncSetAttribute(k_bisect, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need3);
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_tridiag_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need3);
-    if (e != cudaSuccess) return e;
     cur3 = need3;
+  }
+  if (maxn > kClusterBlockedMinN && need_c > cur_c) {
+    e = cudaFuncSetAttribute(k_tridiag_cluster_blocked, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need_c);
+    if (e != cudaSuccess) return e;
+    cur_c = need_c;
   }
   return e;
 }

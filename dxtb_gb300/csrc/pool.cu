@@ -66,7 +66,7 @@ __global__ void k_pool_begin(DevPlan pl, Work w, const int32_t *slots, int n) {
     if (w.phase[m] != kPhaseSetup) continue;  // set-up failed (status says why)
     w.phase[m] = kPhaseIterate;
     w.active_list[act++] = m;
-    if (w.prec[m] != 0 && pl.mol[m].nao > kClusterMinN) w.big64_list[big++] = m;
+    if (cluster_pass(w.prec[m], pl.mol[m].nao)) w.cluster_list[big++] = m;
   }
   w.active[0] = act;
   w.active[1] = big;
@@ -116,7 +116,7 @@ struct gbxtb_pool {
   std::vector<int> state;  // 0 free, 1 admitted (pending), 2 in flight, 3 ended (result ready)
   std::vector<int> pending;
   std::vector<std::vector<double>> pending_pos;
-  int active = 0, big64 = 0;
+  int active = 0, nclus = 0;
   cudaStream_t stream = nullptr;  // stream of the step in flight
   cudaEvent_t done_event = nullptr;  // recorded after the step's last copy
   bool launched = false;
@@ -435,7 +435,7 @@ int gbxtb_pool_step_launch(gbxtb_pool *pool, void *stream) {
     for (int m : pool->pending) {
       pool->state[m] = 2;
       // (upper bounds of the device-side list lengths that k_pool_begin sets)
-      if (!o.mixed_precision && pool->mol[m].nao > kClusterMinN) pool->big64 += 1;
+      if (cluster_pass(o.mixed_precision ? 0 : 1, pool->mol[m].nao)) pool->nclus += 1;
     }
     pool->active += nadm;
     pool->pending.clear();
@@ -443,7 +443,7 @@ int gbxtb_pool_step_launch(gbxtb_pool *pool, void *stream) {
   if (pool->active > 0) {
     // one SCF pass for every iterating slot (the launch shapes of a batch
     // call: few molecules spread over more SMs)
-    const int active = pool->active, big64 = pool->big64;
+    const int active = pool->active, nclus = pool->nclus;
     const bool tail = active <= plan->num_sms;
     launch_gemm(pl, w, plan->tile0, plan->ntile, 6, 0, s);
     if (o.mixed_precision) launch_tridiag_smem(pl, w, s);
@@ -451,7 +451,7 @@ int gbxtb_pool_step_launch(gbxtb_pool *pool, void *stream) {
       launch_tridiag_cluster(pl, w, w.active_list, active, plan->maxn, s);
       launch_bisect(pl, w, plan->maxn, o.kt, w.active_list, active, 32, s);
     } else {
-      if (big64 > 0) launch_tridiag_cluster(pl, w, w.big64_list, big64, plan->maxn, s);
+      if (nclus > 0) launch_tridiag_cluster(pl, w, w.cluster_list, nclus, plan->maxn, s);
       launch_tridiag(pl, w, plan->maxn, s);
       launch_bisect(pl, w, plan->maxn, o.kt, nullptr, pl.nmol, 256, s);
     }
@@ -502,7 +502,7 @@ int gbxtb_pool_step_finish(gbxtb_pool *pool, int32_t *ended, int32_t *nended, in
   }
   *nended = c;
   pool->active = o[pool->nslots + 1];
-  pool->big64 = o[pool->nslots + 2];
+  pool->nclus = o[pool->nslots + 2];
   if (iterating) *iterating = pool->active;
   return GBXTB_OK;
 }

@@ -368,7 +368,7 @@ __global__ void __launch_bounds__(kMixThreads) k_charges_mix(DevParams p, DevPla
 }
 
 // Count and list (in index order) the molecules that still iterate, and
-// among them those whose next pass is FP64 with more than kClusterMinN AOs.
+// among them those whose next pass tridiagonalises on a cluster.
 __device__ __forceinline__ int block_compact(bool flag, int base, int32_t *list, int m, int *wsum) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int act = flag ? 1 : 0;
@@ -391,17 +391,17 @@ __device__ __forceinline__ int block_compact(bool flag, int base, int32_t *list,
 
 __global__ void k_count_active(DevPlan pl, Work w) {
   __shared__ int wsum[32];
-  int base = 0, base64 = 0;
+  int base = 0, basecl = 0;
   for (int m0 = 0; m0 < pl.nmol; m0 += blockDim.x) {
     const int m = m0 + threadIdx.x;
     const bool act = m < pl.nmol && (w.phase[m] == kPhaseIterate || w.phase[m] == kPhaseFinal);
-    const bool big64 = act && w.prec[m] != 0 && pl.mol[m].nao > kClusterMinN;
+    const bool clus = act && cluster_pass(w.prec[m], pl.mol[m].nao);
     base = block_compact(act, base, w.active_list, m, wsum);
-    base64 = block_compact(big64, base64, w.big64_list, m, wsum);
+    basecl = block_compact(clus, basecl, w.cluster_list, m, wsum);
   }
   if (threadIdx.x == 0) {
     w.active[0] = base;
-    w.active[1] = base64;
+    w.active[1] = basecl;
   }
 }
 
