@@ -370,10 +370,10 @@ def main() -> None:
         run_large(args, rank, world, local)
         return
 
-    from dxtb_gb300 import molgen
+    from dxtb_gb300 import replicas
 
     nmol = args.nmol
-    mols = molgen.c2_batch(NMOL, shard=rank)[:nmol]
+    mols = replicas.batch_shard(rank, NMOL)[:nmol]
 
     # host-core baseline first (spawned workers, before any CUDA call)
     cpu = None
@@ -411,11 +411,7 @@ def main() -> None:
             dist.barrier()
 
     def max_over_ranks(x: float) -> float:
-        if world == 1:
-            return x
-        t = torch.tensor([x], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return replicas.max_over_ranks(x, world, dev)
 
     # warm-up
     for _ in range(args.warmup):
@@ -438,7 +434,7 @@ def main() -> None:
         torch.cuda.synchronize()
     barrier()
     t_dev = max_over_ranks(ev0.elapsed_time(ev1) / 1e3)
-    value = nmol * world * args.steps / t_dev
+    value = replicas.whole_job_rate(nmol, world, args.steps, t_dev)
     # stage breakdown of the same call (outside the timed region)
     rp = calc_prof.singlepoint(pos_dev, forces=True)
     prof_ms = dict(calc_prof.last_profile["ms"])
@@ -457,7 +453,7 @@ def main() -> None:
     barrier()
     t_e2e = max_over_ranks(time.perf_counter() - t0)
     nbytes_out = e_host.numel() * 8 + f_host.numel() * 8
-    e2e = nmol * world * args.steps / t_e2e
+    e2e = replicas.whole_job_rate(nmol, world, args.steps, t_e2e)
 
     # the plain per-molecule GPU path: one engine call per molecule
     plain = None
