@@ -455,10 +455,7 @@ __global__ void __launch_bounds__(kTrdThreads) k_tridiag(DevPlan pl, Work w) {
   if (w.prec[m] == 0 || cluster_pass(w.prec[m], md.nao)) return;
   extern __shared__ double sm[];
   __shared__ double red[32];
-  if (w.prec[m])
-    tridiag_body<double>(md, w, sm, red);
-  else
-    tridiag_body<float>(md, w, reinterpret_cast<float *>(sm), reinterpret_cast<float *>(red));
+  tridiag_body<double>(md, w, sm, red);
 }
 
 // ---------------------------------------------------------------------------
@@ -469,10 +466,10 @@ __global__ void __launch_bounds__(kTrdThreads) k_tridiag(DevPlan pl, Work w) {
 // global-memory kernels; this is the kernel of the FP32 passes (most passes
 // of every molecule, all passes of molecules that do not converge).
 // A molecule with more than kSmemLocalMaxN AOs first runs its leading
-// n - kSmemLocalMaxN steps on the FP32 view of A in global memory (same
-// steps as tridiag_body<float>), then loads the trailing matrix on chip.
-// Output conventions as tridiag_body<float>: reflector k in row k of the
-// FP32 view of A (for the back-transformation), d, e, tau in FP64 arrays.
+// n - kSmemLocalMaxN steps on the FP32 view of A in global memory (the
+// steps of tridiag_body), then loads the trailing matrix on chip.
+// Output conventions as tridiag_body: reflector k in row k of the FP32 view
+// of A (for the back-transformation), d, e, tau in FP64 arrays.
 // Launched per size class (kSmemBins) over the plan's per-class molecule
 // lists; molecules of an FP64 pass or already done return at once.
 // ---------------------------------------------------------------------------
@@ -946,7 +943,18 @@ __device__ __forceinline__ void tridiag_cluster_blocked(cg::cluster_group &clust
       T nrm = T(0);
       for (int i = first_own(c + 1) + kClusterSize * tid; i < n; i += kClusterSize * kTrdBlkThreads) {
         T x = A[(int64_t)i * n + c];
-        for (int l = 0; l + 1 < jj; ++l)
+        int l = 0;
+        for (; l + 8 < jj; l += 8) {  // eight pairs of loads in flight
+          T va[8], wa[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            va[u] = ld_cg(A + (int64_t)(p0 + l + u) * n + i);
+            wa[u] = W[(int64_t)(l + u) * n + i];
+          }
+#pragma unroll
+          for (int u = 0; u < 8; ++u) x -= va[u] * coef[l + u] + wa[u] * coef[kPanel + l + u];
+        }
+        for (; l + 1 < jj; ++l)
           x -= ld_cg(A + (int64_t)(p0 + l) * n + i) * coef[l] + W[(int64_t)l * n + i] * coef[kPanel + l];
         if (jj > 0) x -= vs[i - c] * coef[jj - 1] + W[(int64_t)(jj - 1) * n + i] * coef[kPanel + jj - 1];
         xs[i - c - 1] = x;
@@ -957,7 +965,13 @@ __device__ __forceinline__ void tridiag_cluster_blocked(cg::cluster_group &clust
       cluster.sync();
       // --- B: reflector, A22 v and the partial sums -------------------------
       T xn2 = T(0);
-      for (int r = 0; r < kClusterSize; ++r) xn2 += *cluster.map_shared_rank(part + kNorm, r);
+      {
+        T pr[kClusterSize];
+#pragma unroll
+        for (int r = 0; r < kClusterSize; ++r) pr[r] = *cluster.map_shared_rank(part + kNorm, r);
+#pragma unroll
+        for (int r = 0; r < kClusterSize; ++r) xn2 += pr[r];
+      }
       for (int t = tid; t < m1; t += kTrdBlkThreads)
         vs[t] = *cluster.map_shared_rank(xs + t, (c + 1 + t) % kClusterSize);
       __syncthreads();
@@ -978,20 +992,60 @@ __device__ __forceinline__ void tridiag_cluster_blocked(cg::cluster_group &clust
       __syncthreads();  // every thread has read alpha
       for (int t = tid; t < m1; t += kTrdBlkThreads) vs[t] = (t == 0) ? T(1) : vs[t] * scale;
       __syncthreads();
-      // y = A22 v for the own rows, one warp per row, and for row c + 1 in
-      // every CTA (by warp 0, in the same order everywhere)
+      // y = A22 v for the own rows, four rows per warp at a time (two
+      // loads of each in flight per lane), and for row c + 1 in every CTA
+      // (by warp 0, in the same order everywhere)
       T s1 = T(0), s2 = T(0), svav = T(0);  // lane l: partial W^T v, V^T v
       {
+        constexpr int kRows = 4;
+        constexpr int kStride = kClusterSize * NW;  // between a warp's rows
         const int own0 = first_own(c + 1);
-        for (int i = own0 + kClusterSize * wid; i < n; i += kClusterSize * NW) {
-          if (i == c + 1) continue;  // taken below
-          const T acc = row_dot<T, false>(A + (int64_t)i * n + (c + 1), vs, m1, lane);
-          const T vi = vs[i - c - 1];
-          if (lane == 0) ys[i / kClusterSize] = acc;
-          svav += vi * acc;  // identical in every lane
-          if (lane < jj) {
-            s1 += W[(int64_t)lane * n + i] * vi;
-            s2 += ld_cg(A + (int64_t)(p0 + lane) * n + i) * vi;
+        for (int i0 = own0 + kClusterSize * wid; i0 < n; i0 += kRows * kStride) {
+          const T *row[kRows];
+          bool ok[kRows];
+#pragma unroll
+          for (int u = 0; u < kRows; ++u) {
+            const int i = i0 + u * kStride;
+            ok[u] = i < n && i != c + 1;  // row c + 1 is taken below
+            row[u] = A + (int64_t)(ok[u] ? i : i0) * n + (c + 1);
+          }
+          // the W and V entries of these rows (lane l < jj), loaded ahead
+          T wl[kRows], vl[kRows];
+#pragma unroll
+          for (int u = 0; u < kRows; ++u) {
+            const int i = i0 + u * kStride;
+            const bool use = ok[u] && lane < jj;
+            wl[u] = use ? W[(int64_t)lane * n + i] : T(0);
+            vl[u] = use ? ld_cg(A + (int64_t)(p0 + lane) * n + i) : T(0);
+          }
+          T acc[kRows] = {};
+          int t = lane;
+          for (; t + 32 < m1; t += 64) {
+            const T v0 = vs[t], v1 = vs[t + 32];
+            T r0[kRows], r1[kRows];
+#pragma unroll
+            for (int u = 0; u < kRows; ++u) {
+              r0[u] = row[u][t];
+              r1[u] = row[u][t + 32];
+            }
+#pragma unroll
+            for (int u = 0; u < kRows; ++u) acc[u] += r0[u] * v0 + r1[u] * v1;
+          }
+          if (t < m1) {
+            const T v0 = vs[t];
+#pragma unroll
+            for (int u = 0; u < kRows; ++u) acc[u] += row[u][t] * v0;
+          }
+#pragma unroll
+          for (int u = 0; u < kRows; ++u) {
+            const int i = i0 + u * kStride;
+            if (!ok[u]) continue;  // uniform over the warp
+            const T y = warp_sum(acc[u]);
+            const T vi = vs[i - c - 1];
+            if (lane == 0) ys[i / kClusterSize] = y;
+            svav += vi * y;  // identical in every lane
+            s1 += wl[u] * vi;
+            s2 += vl[u] * vi;
           }
         }
       }
@@ -1024,8 +1078,12 @@ __device__ __forceinline__ void tridiag_cluster_blocked(cg::cluster_group &clust
       // --- C: w for the own rows and for row c + 1 ---------------------------
       if (tid <= 2 * kPanel) {
         const int slot = (tid < 2 * kPanel) ? tid : kVav;
+        T pr[kClusterSize];
+#pragma unroll
+        for (int r = 0; r < kClusterSize; ++r) pr[r] = *cluster.map_shared_rank(part + slot, r);
         T s = T(0);
-        for (int r = 0; r < kClusterSize; ++r) s += *cluster.map_shared_rank(part + slot, r);
+#pragma unroll
+        for (int r = 0; r < kClusterSize; ++r) s += pr[r];
         if (tid < 2 * kPanel) x12[tid] = s;
         else coef[2 * kPanel + 1] = s;  // v^T A22 v
       }
@@ -1035,12 +1093,22 @@ __device__ __forceinline__ void tridiag_cluster_blocked(cg::cluster_group &clust
       const T K = tk * (coef[2 * kPanel + 1] - T(2) * x1x2);
       const T half = T(0.5) * tk * K;
       // own rows: w_i = tk (y_i - sum_l V[l][i] x1_l - W[l][i] x2_l) - half v_i
-      for (int i = first_own(c + 2) + kClusterSize * wid; i < n; i += kClusterSize * NW) {
-        T corr = T(0);
-        if (lane < jj)
-          corr = ld_cg(A + (int64_t)(p0 + lane) * n + i) * x12[lane] + W[(int64_t)lane * n + i] * x12[kPanel + lane];
-        corr = warp_sum(corr);
-        if (lane == 0) W[(int64_t)jj * n + i] = tk * (ys[i / kClusterSize] - corr) - half * vs[i - c - 1];
+      // (four rows per warp at a time, their loads in flight together)
+      for (int i0 = first_own(c + 2) + kClusterSize * wid; i0 < n; i0 += 4 * kClusterSize * NW) {
+        T corr[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int i = i0 + u * kClusterSize * NW;
+          corr[u] = (i < n && lane < jj) ? ld_cg(A + (int64_t)(p0 + lane) * n + i) * x12[lane] +
+                                               W[(int64_t)lane * n + i] * x12[kPanel + lane]
+                                         : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int i = i0 + u * kClusterSize * NW;
+          const T cu = warp_sum(corr[u]);
+          if (lane == 0 && i < n) W[(int64_t)jj * n + i] = tk * (ys[i / kClusterSize] - cu) - half * vs[i - c - 1];
+        }
       }
       // row c + 1, in every CTA (warp 0, the same order everywhere)
       if (wid == 0) {
