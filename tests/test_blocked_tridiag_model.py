@@ -1,0 +1,115 @@
+"""A numpy model of the blocked cluster tridiagonalisation
+(``k_tridiag_cluster_blocked`` in ``dxtb_gb300/csrc/linalg.cu``), phase by
+phase in the kernel's order, checked against LAPACK on CPU.
+
+The kernel splits the Householder reduction like LAPACK's dsytrd/dlatrd:
+within a panel of columns the trailing matrix is left as it was at the panel
+start; column c is corrected with the panel's earlier (v, w) pairs before
+its reflector is built; w = tau (A22 v - V (W^T v) - W (V^T v)) - tau/2 (p.v) v;
+and the rank-2 updates are applied at the panel end.  Two details are the
+kernel's own and are modelled here exactly:
+- the previous column's pair enters the next column's correction before any
+  barrier, with its w at row c taken from the value every CTA computes
+  (``wnext``) and its v from the previous reflector still in shared memory;
+- v of column c is stored in row c right of the diagonal, w in the scratch
+  W[l][i] (the eigenvector matrix in the kernel).
+The outputs (d, e, tau and the reflectors) must give Q T Q^T = A with
+Q = H_0 ... H_{n-3}, the back-transformation's convention."""
+import numpy as np
+import pytest
+
+
+def blocked_tridiag(a0: np.ndarray, nb: int):
+    n = a0.shape[0]
+    a = a0.copy()
+    wmat = np.zeros((max(nb, 1), n))
+    d = np.zeros(n)
+    e = np.zeros(n)
+    tau = np.zeros(n)
+    vs = np.zeros(n + 1)
+    wnext = 0.0
+    p0 = 0
+    while p0 + 2 < n:
+        pw = min(nb, n - 2 - p0)
+        for jj in range(pw):
+            c = p0 + jj
+            m1 = n - c - 1
+            # A: row c's coefficients, then the corrected column (own rows)
+            coef_w = np.array([wnext if l == jj - 1 else wmat[l, c] for l in range(jj)])
+            coef_v = np.array([1.0 if l == jj - 1 else a[p0 + l, c] for l in range(jj)])
+            x = np.empty(m1)
+            for i in range(c + 1, n):
+                xi = a[i, c]
+                for l in range(jj - 1):
+                    xi -= a[p0 + l, i] * coef_w[l] + wmat[l, i] * coef_v[l]
+                if jj > 0:
+                    xi -= vs[i - c] * coef_w[jj - 1] + wmat[jj - 1, i] * coef_v[jj - 1]
+                x[i - c - 1] = xi
+            # B: reflector, A22 v, partial sums
+            alpha, xn2 = x[0], float(np.sum(x[1:] ** 2))
+            tk, scale, beta = 0.0, 0.0, alpha
+            if xn2 != 0.0:
+                beta = -np.copysign(np.sqrt(alpha * alpha + xn2), alpha)
+                tk = (beta - alpha) / beta
+                scale = 1.0 / (alpha - beta)
+            d[c] = a[c, c] - 2.0 * float(np.dot(coef_w, coef_v))
+            e[c], tau[c] = beta, tk
+            vs = np.zeros(n + 1)
+            vs[:m1] = x * scale
+            vs[0] = 1.0
+            rows = np.arange(c + 1, n)
+            v = vs[:m1]
+            y = a[c + 1:, c + 1:] @ v
+            x1 = wmat[:jj, rows] @ v          # W^T v
+            x2 = a[p0:p0 + jj, rows] @ v      # V^T v
+            k = tk * (float(v @ y) - 2.0 * float(x1 @ x2))
+            # C: w of every row > c (row c + 1 is the redundant wnext)
+            corr = a[p0:p0 + jj, rows].T @ x1 + wmat[:jj, rows].T @ x2
+            wmat[jj, rows] = tk * (y - corr) - 0.5 * tk * k * v
+            wnext = wmat[jj, c + 1]
+            a[c, c + 1:] = v
+        pe = p0 + pw
+        vp, wp = a[p0:pe, pe:], wmat[:pw, pe:]
+        a[pe:, pe:] -= vp.T @ wp + wp.T @ vp
+        p0 += nb
+    if n >= 2:
+        d[n - 2], d[n - 1], e[n - 2] = a[n - 2, n - 2], a[n - 1, n - 1], a[n - 1, n - 2]
+    else:
+        d[0] = a[0, 0]
+    return d, e[:max(n - 1, 0)], tau, a
+
+
+def q_from_reflectors(a: np.ndarray, tau: np.ndarray) -> np.ndarray:
+    n = a.shape[0]
+    q = np.eye(n)
+    for k in range(n - 3, -1, -1):
+        v = np.zeros(n)
+        v[k + 1:] = a[k, k + 1:]
+        q = q - tau[k] * np.outer(v, v @ q)
+    return q
+
+
+@pytest.mark.parametrize("n,nb", [(2, 32), (3, 32), (5, 2), (12, 4), (40, 8), (70, 32), (97, 32)])
+def test_blocked_model_matches_lapack(n, nb):
+    rng = np.random.default_rng(n)
+    m = rng.normal(size=(n, n))
+    m = (m + m.T) / 2
+    d, e, tau, a = blocked_tridiag(m, nb)
+    t = np.diag(d) + np.diag(e, 1) + np.diag(e, -1)
+    assert np.abs(np.linalg.eigvalsh(t) - np.linalg.eigvalsh(m)).max() < 1e-12
+    if n > 2:
+        q = q_from_reflectors(a, tau)
+        assert np.abs(q @ t @ q.T - m).max() < 1e-12
+
+
+def test_blocked_model_zero_column():
+    # a column that is already reduced (tau = 0, w = 0) inside a panel
+    n = 20
+    rng = np.random.default_rng(3)
+    m = rng.normal(size=(n, n))
+    m = (m + m.T) / 2
+    m[2:, 0] = m[0, 2:] = 0.0
+    d, e, tau, a = blocked_tridiag(m, 8)
+    assert tau[0] == 0.0
+    t = np.diag(d) + np.diag(e, 1) + np.diag(e, -1)
+    assert np.abs(np.linalg.eigvalsh(t) - np.linalg.eigvalsh(m)).max() < 1e-12
