@@ -22,7 +22,8 @@ MOL_NONFINITE = 8
 EXPORTED = (
     "gbxtb_version", "gbxtb_last_error", "gbxtb_ctx_create", "gbxtb_ctx_destroy",
     "gbxtb_plan_create", "gbxtb_plan_destroy", "gbxtb_plan_sizes", "gbxtb_integrals",
-    "gbxtb_singlepoint", "gbxtb_get_status", "gbxtb_get_shell_potential", "gbxtb_get_profile",
+    "gbxtb_singlepoint", "gbxtb_get_status", "gbxtb_get_shell_potential", "gbxtb_get_orbital_charges",
+    "gbxtb_get_profile",
     "gbxtb_fp64_peak", "gbxtb_get_fp32_passes", "gbxtb_singlepoint_noalloc",
     "gbxtb_pool_create", "gbxtb_pool_destroy", "gbxtb_pool_free_slots", "gbxtb_pool_admit",
     "gbxtb_pool_step_launch", "gbxtb_pool_step_finish", "gbxtb_pool_result", "gbxtb_pool_step_poll",
@@ -98,6 +99,7 @@ def load() -> C.CDLL:
     lib.gbxtb_singlepoint.argtypes = [vp, C.POINTER(Options), vp, vp, vp, vp, vp, C.c_size_t, vp]
     lib.gbxtb_get_status.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
     lib.gbxtb_get_shell_potential.argtypes = [vp, C.POINTER(C.c_double)]
+    lib.gbxtb_get_orbital_charges.argtypes = [vp, C.POINTER(C.c_double)]
     lib.gbxtb_get_fp32_passes.argtypes = [vp, C.POINTER(C.c_int32)]
     lib.gbxtb_singlepoint_noalloc.argtypes = [vp, C.POINTER(Options), vp, vp, vp, vp, vp]
     i32p, f64p = C.POINTER(C.c_int32), C.POINTER(C.c_double)
@@ -117,7 +119,7 @@ def load() -> C.CDLL:
     lib.gbxtb_get_profile.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     for name in ("gbxtb_ctx_create", "gbxtb_plan_create", "gbxtb_plan_sizes", "gbxtb_integrals",
                  "gbxtb_singlepoint", "gbxtb_get_status", "gbxtb_get_shell_potential", "gbxtb_get_profile",
-                 "gbxtb_get_fp32_passes", "gbxtb_singlepoint_noalloc", "gbxtb_pool_create",
+                 "gbxtb_get_orbital_charges", "gbxtb_get_fp32_passes", "gbxtb_singlepoint_noalloc", "gbxtb_pool_create",
                  "gbxtb_pool_free_slots", "gbxtb_pool_admit", "gbxtb_pool_step_launch",
                  "gbxtb_pool_step_finish", "gbxtb_pool_result", "gbxtb_pool_step_poll", "gbxtb_plan_autotune"):
         getattr(lib, name).restype = C.c_int

@@ -346,9 +346,59 @@ class GFN1Calculator:
         res = self._run(positions.detach(), chrg, spin, forces=True)
         return -self._pad_vectors(res.gradient)
 
+    def get_potential_energy(self, positions: torch.Tensor, chrg=0, spin=None, **kwargs) -> torch.Tensor:
+        """Alias of ``get_energy`` (``calculators/types/abc.py:101-109``)."""
+        return self.get_energy(positions, chrg, spin, **kwargs)
+
     def get_charges(self, positions: torch.Tensor, chrg=0, spin=None, **kwargs) -> torch.Tensor:
+        """Orbital-resolved Mulliken charges, shape ``(..., nao)`` with
+        padded orbitals set to 0, as ``get_charges`` of the reference
+        (``calculators/types/abc.py:429-486``).  Their sums over each
+        atom's orbitals are the atomic charges of ``singlepoint``."""
+        lib = _lib.load()
+        self._run(positions.detach(), chrg, spin)
+        plan = self._plan(chrg, spin)
+        q = np.zeros(int(plan.sizes[3]))
+        _lib.check(lib.gbxtb_get_orbital_charges(plan.handle, _lib.ptr(q, C.c_double)))
+        return torch.as_tensor(self._pad_orbitals(q), device=self.device)
+
+    def get_mulliken_charges(self, positions: torch.Tensor, chrg=0, spin=None, **kwargs) -> torch.Tensor:
+        """Alias of ``get_charges`` (``calculators/types/abc.py:488-495``)."""
+        return self.get_charges(positions, chrg, spin, **kwargs)
+
+    def get_iterations(self, positions: torch.Tensor, chrg=0, spin=None, **kwargs) -> torch.Tensor:
+        """SCF iterations as a 0-d tensor (``calculators/types/abc.py:497-508``;
+        the reference stores the count of its SCF loop, which for a batch
+        runs until the last molecule is done: here the largest count of the
+        batch)."""
         res = self._run(positions.detach(), chrg, spin)
-        return self._pad_vectors(res.charges)
+        return torch.tensor(int(np.max(res.iterations)), device=self.device)
+
+    def get_implemented_properties(self) -> list[str]:
+        return sorted(["charges", "energy", "forces", "iterations"])
+
+    def _orbital_counts(self) -> np.ndarray:
+        if not hasattr(self, "_nao_per_mol"):
+            elems = params.raw()["elements"]
+            nao_z = {int(z): sum(2 * sh["l"] + 1 for sh in elems[str(int(z))]["shells"])
+                     for z in np.unique(self._numbers_ragged)}
+            per_atom = np.array([nao_z[int(z)] for z in self._numbers_ragged], dtype=np.int64)
+            self._nao_per_mol = np.array([per_atom[self._offsets[m]:self._offsets[m + 1]].sum()
+                                          for m in range(len(self._counts))], dtype=np.int64)
+        return self._nao_per_mol
+
+    def _pad_orbitals(self, ragged: np.ndarray) -> np.ndarray:
+        """Ragged per-orbital values (plan order) -> ``(B, nao_max)``
+        padded with zeros, or ``(nao,)`` for a single molecule."""
+        counts = self._orbital_counts()
+        if len(ragged) != int(counts.sum()):
+            raise ValueError(f"{len(ragged)} orbital values for {int(counts.sum())} orbitals")
+        out = np.zeros((len(counts), int(counts.max())))
+        off = 0
+        for m, n in enumerate(counts):
+            out[m, :n] = ragged[off:off + n]
+            off += n
+        return out if self.batched else out[0]
 
     def get_integrals(self, positions: torch.Tensor, chrg=0, spin=None):
         """Overlap and core Hamiltonian of every molecule, as a list of

@@ -742,4 +742,11 @@ int gbxtb_get_shell_potential(gbxtb_plan *plan, double *potential) {
   return GBXTB_OK;
 }
 
+int gbxtb_get_orbital_charges(gbxtb_plan *plan, double *charges) {
+  if (!plan || !plan->has_run || !charges) return fail(GBXTB_ERR_ARG, "no singlepoint has run on this plan");
+  CK(cudaStreamSynchronize(plan->last_stream));
+  CK(cudaMemcpy(charges, plan->last_work.q, sizeof(double) * plan->pl.nao, cudaMemcpyDeviceToHost));
+  return GBXTB_OK;
+}
+
 }  // extern "C"

@@ -195,6 +195,14 @@ GBXTB_API int gbxtb_get_profile(gbxtb_plan *plan, double *ms, int64_t *launches,
  * over the 2l+1 orbitals of each shell.  Synchronises that call's stream. */
 GBXTB_API int gbxtb_get_shell_potential(gbxtb_plan *plan, double *potential);
 
+/* Orbital-resolved Mulliken charges q_mu = n0_mu - (P S)_mu,mu of the final
+ * state of the last gbxtb_singlepoint (host array of naos, in plan order);
+ * replaces get_charges / get_mulliken_charges (calculators/types/abc.py:
+ * 429-495, the `mono` charges of scf/base.py:764-815).  The atomic charges
+ * that gbxtb_singlepoint writes are their sums over each atom's orbitals.
+ * Synchronises that call's stream. */
+GBXTB_API int gbxtb_get_orbital_charges(gbxtb_plan *plan, double *charges);
+
 /* ---------------------------------------------------------------------------
  * Slot pool: continuous batching of single points with forces (serving).
  * A pool holds nslots molecules of up to cap_atoms atoms, cap_shells shells

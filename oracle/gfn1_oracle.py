@@ -558,6 +558,7 @@ class Result:
     converged: bool
     forces: np.ndarray | None = None
     emo: np.ndarray | None = None
+    charges_orbital: np.ndarray | None = None  # q per AO before the reduction to atoms
 
 
 class Broyden:
@@ -706,6 +707,7 @@ def singlepoint(numbers, positions, chrg: float = 0.0, spin=None, forces: bool =
         energy=float(eat.sum()), energy_atoms=eat, e_rep=float(erep_at.sum()),
         e_h0=float(e_h0.sum()), e_es2=float(e_es2.sum()), e_es3=float(e_es3.sum()),
         e_fermi=g, charges=qat, iterations=it, converged=converged, emo=state["emo"],
+        charges_orbital=q,
     )
     if forces:
         v_orb = charges_to_pot(q)

@@ -97,6 +97,36 @@ def test_engine_replays_oracle_broyden():
         assert abs(int(res.iterations[0]) - r.iterations) <= 2
 
 
+def test_orbital_charges():
+    """get_charges gives orbital-resolved Mulliken charges, as the
+    reference's get_charges (calculators/types/abc.py:429-486): they match
+    the oracle's per-orbital charges, their sums over each atom's orbitals
+    are the atomic charges of singlepoint, and a batch pads them with 0."""
+    mols = molgen.c3_forces(2)
+    num, pos = pad(mols)
+    calc = calc_for(num)
+    p = torch.tensor(pos, device="cuda")
+    q = calc.get_charges(p).cpu().numpy()
+    assert torch.equal(calc.get_mulliken_charges(p).cpu(), torch.as_tensor(q))
+    qat = calc.singlepoint(p).charges.cpu().numpy()
+    naos = []
+    off = 0
+    for k, (n1, p1) in enumerate(mols):
+        r = go.singlepoint(n1, p1, mixer="broyden", forces=False)
+        nao = len(r.charges_orbital)
+        naos.append(nao)
+        assert np.abs(q[k, :nao] - r.charges_orbital).max() < Q_TOL
+        assert np.all(q[k, nao:] == 0.0)
+        b = go.Basis(n1)
+        sums = np.bincount(b.sh_atom[b.ao_sh], weights=q[k, :nao], minlength=len(n1))
+        assert np.abs(sums - qat[off:off + len(n1)]).max() < 1e-12
+        off += len(n1)
+    assert q.shape == (2, max(naos))
+    # a single molecule gives a vector
+    q1 = calc_for(mols[0][0]).get_charges(torch.tensor(mols[0][1], device="cuda"))
+    assert q1.shape == (naos[0],)
+
+
 def test_batch_equals_single():
     mols = molgen.c2_batch(6)
     num, pos = pad(mols)

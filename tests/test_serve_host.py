@@ -32,3 +32,33 @@ def test_latency_summary():
     s = serve.latency_summary(reqs)
     assert abs(s["p50_ms"] - 50.5) < 1e-9
     assert 99.0 <= s["p99_ms"] <= 100.0
+
+
+def test_orbital_padding_of_the_calculator():
+    """The host-side padding of per-orbital values (get_charges): ragged in
+    plan order -> (B, nao_max) with zeros, or (nao,) for one molecule."""
+    import numpy as np
+
+    from dxtb_gb300.calculator import GFN1Calculator
+
+    calc = GFN1Calculator.__new__(GFN1Calculator)  # no device needed for the padding
+    calc._numbers_ragged = np.array([8, 1, 1, 6, 1, 1, 1, 1])  # H2O, CH4
+    calc._counts = np.array([3, 5])
+    calc._offsets = np.array([0, 3, 8])
+    calc.batched = True
+    assert calc._orbital_counts().tolist() == [8, 12]
+    ragged = np.arange(20.0)
+    out = calc._pad_orbitals(ragged)
+    assert out.shape == (2, 12)
+    assert out[0, :8].tolist() == list(range(8)) and np.all(out[0, 8:] == 0)
+    assert out[1].tolist() == list(range(8, 20))
+    single = GFN1Calculator.__new__(GFN1Calculator)
+    single._numbers_ragged = np.array([8, 1, 1])
+    single._counts = np.array([3])
+    single._offsets = np.array([0, 3])
+    single.batched = False
+    assert single._pad_orbitals(np.ones(8)).shape == (8,)
+    import pytest
+
+    with pytest.raises(ValueError):
+        calc._pad_orbitals(np.ones(19))
