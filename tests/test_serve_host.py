@@ -1,5 +1,8 @@
 """Host-side pieces of the serving layer (no GPU): size classes, slot
-memory footprint, latency statistics."""
+memory footprint, latency statistics, and the admission and step logic of
+``Server`` over stand-in pools."""
+import time
+
 import numpy as np
 
 from dxtb_gb300 import serve
@@ -62,3 +65,88 @@ def test_orbital_padding_of_the_calculator():
 
     with pytest.raises(ValueError):
         calc._pad_orbitals(np.ones(19))
+
+
+class _FakePool:
+    """Stands in for a slot pool: a fixed number of slots; a launched step
+    ends the molecules whose remaining pass count reaches 0."""
+
+    def __init__(self, max_atoms, nslots, passes=2):
+        self.max_atoms, self.nslots, self.passes = max_atoms, nslots, passes
+        self.requests = {}
+        self.left = {}
+        self.launched = False
+        self.iterating = 0
+
+    def free(self):
+        return self.nslots - len(self.requests)
+
+    def admit(self, req):
+        if self.free() == 0:
+            return False
+        slot = min(set(range(self.nslots)) - set(self.requests))
+        self.requests[slot] = req
+        self.left[slot] = self.passes
+        return True
+
+    def launch(self):
+        self.launched = True
+
+    def ready(self):
+        return True
+
+    def finish(self):
+        self.launched = False
+        done = []
+        for slot in list(self.requests):
+            self.left[slot] -= 1
+            if self.left[slot] == 0:
+                req = self.requests.pop(slot)
+                req.energy, req.status, req.iterations = -1.0, 0, self.passes
+                req.t_left = time.perf_counter()  # the slot is free from here on
+                done.append(req)
+        return done
+
+    @property
+    def busy(self):
+        return bool(self.requests)
+
+
+def _server_with_fake_pools(classes):
+    srv = serve.Server.__new__(serve.Server)
+    srv.pools = [_FakePool(a, n) for a, n in classes]
+    srv.queue = serve.deque()
+    srv.completed = []
+    srv._next_id = 0
+    srv.steps = 0
+    srv.device = 0
+    return srv
+
+
+def test_requests_go_to_the_smallest_class_that_fits_and_wait_when_full():
+    srv = _server_with_fake_pools([(10, 1), (40, 2)])
+    sizes = [5, 30, 8, 35, 3]
+    for n in sizes:
+        srv.submit(np.ones(n, dtype=np.int64), np.zeros((n, 3)))
+    srv.step(wait=False)
+    # the 5-atom one in the small class, 30 and 8 in the large class (the
+    # small class is full), 35 and 3 wait
+    placed = {r.id: r.size_class for p in srv.pools for r in p.requests.values()}
+    assert placed == {0: 0, 1: 1, 2: 1}
+    assert [r.id for r in srv.queue] == [3, 4]
+    srv.run_until_idle()
+    assert srv.idle
+    assert sorted(r.id for r in srv.completed) == list(range(len(sizes)))
+    assert all(r.status == 0 and r.latency is not None for r in srv.completed)
+    # the waiting requests took slots that others had left: continuous batching
+    by_id = {r.id: r for r in srv.completed}
+    first_left = min(by_id[k].t_left for k in (0, 1, 2))
+    assert by_id[3].t_admit >= first_left and by_id[4].t_admit >= first_left
+
+
+def test_oversized_request_is_refused_on_the_host():
+    import pytest
+
+    srv = _server_with_fake_pools([(10, 1)])
+    with pytest.raises(ValueError):
+        srv.submit(np.ones(11, dtype=np.int64), np.zeros((11, 3)))
