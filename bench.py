@@ -153,7 +153,8 @@ class ClockSampler:
 def flop_model(plan_n: np.ndarray, kocc: np.ndarray, passes: np.ndarray, passes32: np.ndarray) -> dict:
     """Algorithmic flops per kernel class for the whole call, split into the
     FP64 and FP32 passes of every molecule (the frozen work model): per
-    pass, Householder tridiagonalisation of the full matrix 2 N^3, Fock
+    pass, Householder tridiagonalisation 4/3 N^3 (the symmetric count; the
+    kernels on full storage do 2 N^3, which is not credited), Fock
     transform L^-1 diag(v) L 1/3 N^3, back-transformation 2 N^2 k, density
     (C = L^-T Y and P = C f C^T) 2 N^2 k; per geometry Cholesky + L^-1
     2/3 N^3 and L^-1 H0 L^-T 3 N^3.  k = occupied orbitals."""
@@ -162,7 +163,7 @@ def flop_model(plan_n: np.ndarray, kocc: np.ndarray, passes: np.ndarray, passes3
     p32 = passes32.astype(np.float64)
     p64 = passes.astype(np.float64) - p32
     per_pass = {
-        "tridiag": 2.0 * n ** 3,
+        "tridiag": 4.0 / 3.0 * n ** 3,
         "fock": n ** 3 / 3.0,
         "backtransform": 2.0 * n * n * k,
         "density": 2.0 * n * n * k,
