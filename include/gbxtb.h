@@ -92,7 +92,8 @@ typedef struct {
   double broyden_alpha;   /* mixer step */
   int32_t profile;        /* 1: time each kernel class with CUDA events (gbxtb_get_profile) */
   int32_t mixed_precision; /* 1: SCF passes run their linear algebra in FP32 while the
-                              potential change is above 1e-4 (at most 40 passes);
+                              potential change is above 1e-4 and still falling
+                              (8 passes without halving below 1e-3 end them);
                               convergence and the final state are always FP64.
                               0: every pass in FP64 */
 } gbxtb_options;
