@@ -236,7 +236,11 @@ def run_large(args, rank: int, world: int, local: int) -> None:
     import warnings
 
     warnings.simplefilter("ignore")
-    mols = molgen.c5_large(16)[: args.large]
+    if args.large_atoms:
+        # single grown molecules of the given atom counts (seed 7000 + atoms)
+        mols = [molgen.grow(int(a), 7000 + int(a)) for a in args.large_atoms.split(",")]
+    else:
+        mols = molgen.c5_large(16)[: args.large]
     num, pos = pad(mols)
     calc = GFN1Calculator(torch.as_tensor(num), opts={**OPTS, "profile": True})
     p = torch.tensor(pos, device="cuda")
@@ -251,8 +255,10 @@ def run_large(args, rank: int, world: int, local: int) -> None:
         "metric": METRIC, "value": len(mols) / dt, "unit": UNIT, "n_gpus": world, "steps": 1, "warmup": 0,
         "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded CHNO molecules)",
-        "config": {"workload": f"{len(mols)} of the 16 large molecules, 1000-2000 atoms, energy + forces, "
-                               "SCF |dv|<1e-10, one call", "atoms": [int(len(a)) for a, _ in mols],
+        "config": {"workload": (f"grown molecules of {args.large_atoms} atoms" if args.large_atoms else
+                                f"{len(mols)} of the 16 large molecules, 1000-2000 atoms")
+                               + ", energy + forces, SCF |dv|<1e-10, one call",
+                   "atoms": [int(len(a)) for a, _ in mols],
                    "basis_functions": [int(x) for x in n]},
         "iterations": res.iterations.tolist(), "fp32_passes": res.fp32_passes.tolist(),
         "status": res.status.tolist(), "stage_ms": calc.last_profile["ms"], "clocks": clk.summary(),
@@ -353,6 +359,8 @@ def main() -> None:
     ap.add_argument("--serve-rates", default="100,200,500,1000,2000,5000", help="arrival rates (req/s)")
     ap.add_argument("--large", type=int, default=0, metavar="K",
                     help="large molecules instead of the batch: K of the 16 molecules of 1000-2000 atoms")
+    ap.add_argument("--large-atoms", default="", metavar="N1,N2",
+                    help="large-molecule mode on single grown molecules of these atom counts")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -367,7 +375,7 @@ def main() -> None:
     if args.serve:
         run_serve(args, rank, world, local)
         return
-    if args.large:
+    if args.large or args.large_atoms:
         run_large(args, rank, world, local)
         return
 
