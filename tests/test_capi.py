@@ -44,3 +44,44 @@ def test_version_and_errors(lib):
     ws = C.c_size_t()
     assert lib.gbxtb_plan_create(None, 0, None, None, None, None, C.byref(h), C.byref(ws)) == -1
     assert lib.gbxtb_get_status(None, None, None) == -1
+
+
+def test_null_arguments_of_every_entry_point(lib):
+    """Each entry point refuses null handles and buffers with
+    GBXTB_ERR_ARG (-1) and a message, before any device call."""
+    from dxtb_gb300 import _lib
+
+    opts = _lib.Options()
+    h = C.c_void_p()
+    n = C.c_size_t()
+    i32 = C.c_int32()
+    calls = {
+        "gbxtb_integrals": lambda: lib.gbxtb_integrals(None, None, None, None, None, 0, None),
+        "gbxtb_singlepoint": lambda: lib.gbxtb_singlepoint(None, None, None, None, None, None, None, 0, None),
+        "gbxtb_singlepoint_noalloc": lambda: lib.gbxtb_singlepoint_noalloc(None, None, None, None, None, None,
+                                                                           None),
+        "gbxtb_plan_autotune": lambda: lib.gbxtb_plan_autotune(None, C.byref(opts), None, None, 0, None, None),
+        "gbxtb_get_fp32_passes": lambda: lib.gbxtb_get_fp32_passes(None, None),
+        "gbxtb_get_shell_potential": lambda: lib.gbxtb_get_shell_potential(None, None),
+        "gbxtb_get_orbital_charges": lambda: lib.gbxtb_get_orbital_charges(None, None),
+        "gbxtb_get_profile": lambda: lib.gbxtb_get_profile(None, None, None, None),
+        "gbxtb_pool_create": lambda: lib.gbxtb_pool_create(None, C.byref(opts), 1, 1, 1, 1, C.byref(h),
+                                                           C.byref(n)),
+        "gbxtb_pool_admit": lambda: lib.gbxtb_pool_admit(None, 1, None, None, 0.0, -1, C.byref(i32)),
+        "gbxtb_pool_step_launch": lambda: lib.gbxtb_pool_step_launch(None, None),
+        "gbxtb_pool_result": lambda: lib.gbxtb_pool_result(None, 0, None, None, None, None, None),
+    }
+    for name, call in calls.items():
+        assert call() == _lib.GBXTB_OK - 1, name
+        assert lib.gbxtb_last_error(), name
+
+
+def test_missing_library_fails_loudly(monkeypatch, tmp_path):
+    """Without the built engine the package refuses to run: there is no CPU
+    fallback."""
+    from dxtb_gb300 import _lib
+
+    monkeypatch.setattr(_lib, "_lib", None)
+    monkeypatch.setattr(_lib, "LIB_PATH", tmp_path / "libgbxtb.so")
+    with pytest.raises(_lib.GbxtbError, match="no CPU fallback"):
+        _lib.load()
