@@ -27,7 +27,7 @@ EXPORTED = (
     "gbxtb_fp64_peak", "gbxtb_get_fp32_passes", "gbxtb_singlepoint_noalloc",
     "gbxtb_pool_create", "gbxtb_pool_destroy", "gbxtb_pool_free_slots", "gbxtb_pool_admit",
     "gbxtb_pool_step_launch", "gbxtb_pool_step_finish", "gbxtb_pool_result", "gbxtb_pool_step_poll",
-    "gbxtb_plan_autotune",
+    "gbxtb_plan_autotune", "gbxtb_default_options", "gbxtb_forces",
 )
 
 NOALLOC_SCRATCH_BYTES = 32 * 1024 * 1024  # GBXTB_NOALLOC_SCRATCH_BYTES
@@ -62,7 +62,31 @@ class Options(C.Structure):
         ("broyden_alpha", C.c_double),
         ("profile", C.c_int32),
         ("mixed_precision", C.c_int32),
+        ("mixer", C.c_int32),
+        ("generations", C.c_int32),
+        ("damp", C.c_double),
+        ("damp_init", C.c_double),
+        ("diagonal_offset", C.c_double),
+        ("soft_start", C.c_int32),
+        ("mix_guess", C.c_int32),
+        ("damp_dynamic", C.c_int32),
+        ("reserved", C.c_int32),
+        ("damp_dynamic_factor", C.c_double),
+        ("fermi_thresh", C.c_double),
     ]
+
+
+MIXER_BROYDEN = 0
+MIXER_ANDERSON = 1
+MIXER_SIMPLE = 2
+MIXERS = {"broyden": MIXER_BROYDEN, "anderson": MIXER_ANDERSON, "simple": MIXER_SIMPLE}
+
+
+def default_options() -> "Options":
+    """Options filled by ``gbxtb_default_options`` (the reference's defaults)."""
+    o = Options()
+    load().gbxtb_default_options(C.byref(o))
+    return o
 
 
 class GbxtbError(RuntimeError):
@@ -85,6 +109,10 @@ def load() -> C.CDLL:
     lib = C.CDLL(str(LIB_PATH))
     vp = C.c_void_p
     lib.gbxtb_version.restype = C.c_int
+    lib.gbxtb_default_options.argtypes = [C.POINTER(Options)]
+    lib.gbxtb_default_options.restype = None
+    lib.gbxtb_forces.argtypes = [vp, vp, vp, vp, C.c_size_t, vp]
+    lib.gbxtb_forces.restype = C.c_int
     lib.gbxtb_last_error.restype = C.c_char_p
     lib.gbxtb_ctx_create.argtypes = [C.POINTER(Params), C.POINTER(vp)]
     lib.gbxtb_ctx_destroy.argtypes = [vp]

@@ -1,8 +1,12 @@
-"""Build ``libgbxtb.so`` (the CUDA engine and its C ABI) in-tree for sm_103a.
+"""Build ``libgbxtb.so`` (the CUDA engine and its C ABI) in-tree for sm_103a,
+and the torch operators over it.
 
 ``python -m dxtb_gb300.build`` compiles every ``csrc/*.cu`` translation unit
-in parallel with nvcc and links them into ``dxtb_gb300/libgbxtb.so``.
-Objects go to ``dxtb_gb300/_build/`` (git-ignored).
+in parallel with nvcc and links them into ``dxtb_gb300/libgbxtb.so``; then
+``csrc/torch_ops.cpp`` (``TORCH_LIBRARY(gbxtb, m)``: ``torch.ops.gbxtb.*``)
+is compiled against torch and that library into
+``dxtb_gb300/_build/torch_ops/gbxtb_torch_ops.so``.  Objects go to
+``dxtb_gb300/_build/`` (git-ignored).
 """
 from __future__ import annotations
 
@@ -28,6 +32,39 @@ def nvcc() -> str:
         if cand and Path(cand).exists():
             return cand
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libgbxtb.so")
+
+
+TORCH_OPS_SRC = CSRC / "torch_ops.cpp"
+TORCH_OPS_DIR = BUILD / "torch_ops"
+TORCH_OPS_NAME = "gbxtb_torch_ops"
+
+
+def torch_ops_path() -> Path:
+    return TORCH_OPS_DIR / f"{TORCH_OPS_NAME}.so"
+
+
+def build_torch_ops(verbose: bool = False) -> Path:
+    """Compile and load the torch operators (needs libgbxtb.so built)."""
+    from torch.utils import cpp_extension
+
+    out = torch_ops_path()
+    deps = [TORCH_OPS_SRC, PKG.parent / "include" / "gbxtb.h", LIB]
+    if out.exists() and any(d.exists() and d.stat().st_mtime > out.stat().st_mtime for d in deps):
+        shutil.rmtree(TORCH_OPS_DIR)  # the C ABI changed: rebuild from scratch
+    TORCH_OPS_DIR.mkdir(parents=True, exist_ok=True)
+    cuda_home = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
+    cpp_extension.load(
+        name=TORCH_OPS_NAME,
+        sources=[str(TORCH_OPS_SRC)],
+        extra_cflags=["-O2"],
+        extra_include_paths=[str(PKG.parent / "include"), str(cuda_home / "include")],
+        extra_ldflags=[f"-L{PKG}", "-lgbxtb", f"-Wl,-rpath,{PKG}"],
+        build_directory=str(TORCH_OPS_DIR),
+        with_cuda=True,
+        is_python_module=False,
+        verbose=verbose,
+    )
+    return torch_ops_path()
 
 
 def _sources() -> list[Path]:
@@ -62,7 +99,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | N
     with ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 1)) as ex:
         objs = list(ex.map(compile_one, _sources()))
     tmp = LIB.with_suffix(".so.tmp")
-    cmd = [cc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs)]
+    cmd = [cc, *ARCH, "-shared", "-Xlinker", "-soname=libgbxtb.so", "-o", str(tmp), *map(str, objs)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
@@ -72,3 +109,5 @@ def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | N
 
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    if "--no-torch-ops" not in sys.argv:
+        print(build_torch_ops(verbose="-v" in sys.argv))

@@ -87,11 +87,68 @@ int describe_molecule(const gbxtb_ctx *ctx, const int32_t *numbers, int natoms, 
 
 int set_error(int code, const std::string &msg) { return fail(code, msg); }
 size_t plan_workspace_bytes(const gbxtb_plan *plan) { return plan ? plan->ws_bytes : 0; }
+int plan_device(const gbxtb_plan *plan) { return plan ? plan->ctx->device : -1; }
+
+int check_options(const gbxtb_options *o) {
+  if (!o) return fail(GBXTB_ERR_ARG, "null options");
+  if (o->maxiter < 0) return fail(GBXTB_ERR_ARG, "maxiter must be >= 0");
+  if (o->fermi_maxiter < 1) return fail(GBXTB_ERR_ARG, "fermi_maxiter must be >= 1");
+  if (!(o->kt > 0.0)) return fail(GBXTB_ERR_ARG, "the electronic temperature must be positive");
+  if (!(std::isfinite(o->x_atol) && std::isfinite(o->x_atol_max)))
+    return fail(GBXTB_ERR_ARG, "x_atol and x_atol_max must be finite");
+  switch (o->mixer) {
+    case GBXTB_MIXER_BROYDEN:
+      if (o->broyden_memory < 1 || o->broyden_memory > kHistMax)
+        return fail(GBXTB_ERR_ARG, "broyden_memory must be in 1.." + std::to_string(kHistMax));
+      if (!std::isfinite(o->broyden_alpha)) return fail(GBXTB_ERR_ARG, "broyden_alpha must be finite");
+      break;
+    case GBXTB_MIXER_ANDERSON:
+      if (o->generations < 1 || o->generations > kHistMax - 1)
+        return fail(GBXTB_ERR_ARG, "generations must be in 1.." + std::to_string(kHistMax - 1));
+      if (!(std::isfinite(o->damp) && std::isfinite(o->damp_init) && std::isfinite(o->diagonal_offset)))
+        return fail(GBXTB_ERR_ARG, "damp, damp_init and diagonal_offset must be finite");
+      break;
+    case GBXTB_MIXER_SIMPLE:
+      if (!std::isfinite(o->damp)) return fail(GBXTB_ERR_ARG, "damp must be finite");
+      break;
+    default:
+      return fail(GBXTB_ERR_ARG, "unknown mixer " + std::to_string(o->mixer));
+  }
+  if (!std::isfinite(o->fermi_thresh)) return fail(GBXTB_ERR_ARG, "fermi_thresh must be finite");
+  if (o->damp_dynamic && !std::isfinite(o->damp_dynamic_factor))
+    return fail(GBXTB_ERR_ARG, "damp_dynamic_factor must be finite");
+  return GBXTB_OK;
+}
 }  // namespace gbxtb
 
 extern "C" {
 
 int gbxtb_version(void) { return GBXTB_VERSION; }
+
+void gbxtb_default_options(gbxtb_options *o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->maxiter = 100;
+  o->fermi_maxiter = 200;
+  o->broyden_memory = 20;
+  o->want_forces = 0;
+  o->x_atol = 1.0e-4;
+  o->x_atol_max = 1.0e-5;
+  o->kt = 300.0 * (1.3806488e-23 / 4.35974434e-18);  // 300 K in Hartree: k_B / E_h (CODATA 2010)
+  o->broyden_alpha = 0.3;
+  o->profile = 0;
+  o->mixed_precision = 0;
+  o->mixer = GBXTB_MIXER_ANDERSON;
+  o->generations = 5;
+  o->damp = 0.5;
+  o->damp_init = 0.1;
+  o->diagonal_offset = 0.01;
+  o->soft_start = 1;
+  o->mix_guess = 1;
+  o->damp_dynamic = 0;
+  o->damp_dynamic_factor = 0.99;
+  o->fermi_thresh = 0.0;
+}
 
 const char *gbxtb_last_error(void) { return g_err.c_str(); }
 
@@ -369,6 +426,8 @@ int gbxtb_integrals(gbxtb_plan *plan, const double *positions_dev, double *overl
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const DevPlan &pl = plan->pl;
   const DevParams &p = plan->ctx->p;
+  CK(cudaMemsetAsync(w.status, 0, sizeof(int32_t) * pl.nmol, s));
+  CK(cudaMemsetAsync(w.phase, 0, sizeof(int32_t) * pl.nmol, s));
   launch_atoms(p, pl, w, positions_dev, false, s);
   launch_shellpairs(p, pl, w, positions_dev, s);
   CK(cudaGetLastError());
@@ -424,6 +483,8 @@ int enqueue_setup(gbxtb_plan *plan, const Work &w, const gbxtb_options &o, const
   CK(cudaMemsetAsync(w.nhist, 0, sizeof(int32_t) * pl.nmol, s));
   CK(cudaMemsetAsync(w.npass32, 0, sizeof(int32_t) * pl.nmol, s));
   CK(cudaMemsetAsync(w.stall32, 0, sizeof(int32_t) * pl.nmol, s));
+  CK(cudaMemsetAsync(w.mixstep, 0, sizeof(int32_t) * pl.nmol, s));
+  CK(cudaMemsetAsync(w.dampsw, 0, sizeof(int32_t) * pl.nmol, s));
   CK(cudaMemsetAsync(w.best32, 0x7f, sizeof(double) * pl.nmol, s));  // 1.4e306: no pass yet
   // 0: the first passes run in FP32; any non-zero byte pattern means FP64
   CK(cudaMemsetAsync(w.prec, opts->mixed_precision ? 0 : 1, sizeof(int32_t) * pl.nmol, s));
@@ -457,7 +518,6 @@ int enqueue_pass(gbxtb_plan *plan, const Work &w, const gbxtb_options &o, bool t
   const DevPlan &pl = plan->pl;
   const DevParams &p = plan->ctx->p;
   const gbxtb_options *opts = &o;
-  const int it = 0;
   Prof none{plan, s, false};
   Prof &prof = pf ? *pf : none;
   const int64_t before = plan->total_launches;
@@ -485,7 +545,7 @@ int enqueue_pass(gbxtb_plan *plan, const Work &w, const gbxtb_options &o, bool t
     launch_bisect(pl, w, plan->maxn, opts->kt, nullptr, pl.nmol, pl.bisect_threads, s);
   prof.end(GBXTB_PROF_BISECT, 1);
   prof.begin(GBXTB_PROF_FERMI);
-  launch_fermi(pl, w, opts->kt, opts->fermi_maxiter, s);
+  launch_fermi(pl, w, opts->kt, opts->fermi_maxiter, opts->fermi_thresh, s);
   prof.end(GBXTB_PROF_FERMI, 1);
   prof.begin(GBXTB_PROF_INVIT);
   launch_invit(pl, w, plan->maxn, s);
@@ -501,10 +561,9 @@ int enqueue_pass(gbxtb_plan *plan, const Work &w, const gbxtb_options &o, bool t
   launch_gemm(pl, w, plan->tile0, plan->ntile, 3, 0, s);
   prof.end(GBXTB_PROF_DENSITY, 2);
   prof.begin(GBXTB_PROF_MIX);
-  launch_charges_mix(p, pl, w, *opts, it, s);
+  launch_charges_mix(p, pl, w, *opts, s);
   launch_count_active(pl, w, s);
   prof.end(GBXTB_PROF_MIX, 2);
-  (void)it;
   const int n = (int)(plan->total_launches - before);
   if (!pf) plan->total_launches = before;  // counted when the graph is launched
   return n;
@@ -516,9 +575,7 @@ int gbxtb_singlepoint(gbxtb_plan *plan, const gbxtb_options *opts, const double 
                       void *workspace_dev, size_t workspace_bytes, void *stream) {
   if (!opts || !energy_dev) return fail(GBXTB_ERR_ARG, "null argument");
   if (opts->want_forces && !gradient_dev) return fail(GBXTB_ERR_ARG, "forces requested without gradient buffer");
-  if (opts->maxiter < 0 || opts->fermi_maxiter < 1 || !(opts->kt > 0.0) || opts->broyden_memory < 1 ||
-      opts->broyden_memory > kHistMax)
-    return fail(GBXTB_ERR_ARG, "invalid options");
+  if (const int orc = check_options(opts)) return orc;
   Work w;
   int rc = prepare(plan, positions_dev, workspace_dev, workspace_bytes, w);
   if (rc) return rc;
@@ -623,13 +680,32 @@ int gbxtb_singlepoint(gbxtb_plan *plan, const gbxtb_options *opts, const double 
   }
   plan->last_stream = s;
   plan->last_work = w;
+  plan->last_ws = workspace_dev;
   plan->has_run = true;
+  return GBXTB_OK;
+}
+
+int gbxtb_forces(gbxtb_plan *plan, const double *positions_dev, double *gradient_dev, void *workspace_dev,
+                 size_t workspace_bytes, void *stream) {
+  if (!gradient_dev) return fail(GBXTB_ERR_ARG, "null argument");
+  if (!plan || !plan->has_run) return fail(GBXTB_ERR_ARG, "no singlepoint has run on this plan");
+  if (workspace_dev != plan->last_ws)
+    return fail(GBXTB_ERR_ARG, "the workspace is not the one of the plan's last singlepoint");
+  Work w;
+  const int rc = prepare(plan, positions_dev, workspace_dev, workspace_bytes, w);
+  if (rc) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  launch_gemm(plan->pl, w, plan->tile0, plan->ntile, 4, 1, s);
+  launch_forces(plan->ctx->p, plan->pl, w, positions_dev, gradient_dev, s);
+  CK(cudaGetLastError());
+  plan->last_stream = s;
   return GBXTB_OK;
 }
 
 int gbxtb_plan_autotune(gbxtb_plan *plan, const gbxtb_options *opts, const double *positions_dev,
                         void *workspace_dev, size_t workspace_bytes, void *stream, int32_t *choice) {
   if (!opts) return fail(GBXTB_ERR_ARG, "null argument");
+  if (const int orc = check_options(opts)) return orc;
   Work w;
   int rc = prepare(plan, positions_dev, workspace_dev, workspace_bytes, w);
   if (rc) return rc;

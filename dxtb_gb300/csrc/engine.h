@@ -56,7 +56,7 @@ int describe_molecule(const gbxtb_ctx *ctx, const int32_t *numbers, int natoms, 
 
 namespace gbxtb {
 inline size_t align256(size_t x) { return (x + 255) / 256 * 256; }
-constexpr int kHistMax = 29;  // longest mixer history
+constexpr int kHistMax = 29;  // longest mixer history (Broyden pairs; Anderson generations + 1)
 }  // namespace gbxtb
 
 struct gbxtb_ctx {
@@ -79,6 +79,7 @@ struct gbxtb_plan {
   // state of the last singlepoint
   cudaStream_t last_stream = nullptr;
   gbxtb::Work last_work{};
+  void *last_ws = nullptr;  // workspace of the last singlepoint (its final SCF state)
   bool has_run = false;
   int32_t *h_active = nullptr;  // pinned
   int num_sms = 0;
@@ -126,7 +127,7 @@ inline Layout make_layout(const DevPlan &pl) {
   L.add(d * pl.ngam);                                       // gam
   for (int k = 0; k < 4; ++k) L.add(d * pl.natom);          // cn erep qat dedcn
   L.add(d * 3 * pl.natom);                                  // grad
-  for (int k = 0; k < 8; ++k) L.add(i4 * pl.nmol);          // status phase iter kvec nhist prec npass32 stall32
+  for (int k = 0; k < 10; ++k) L.add(i4 * pl.nmol);  // status phase iter kvec nhist prec npass32 stall32 mixstep dampsw
   L.add(d * 2 * pl.nmol);                                   // efermi
   L.add(d * 6 * pl.nmol);                                   // energy
   L.add(d * 2 * pl.nmol);                                   // resid
@@ -156,6 +157,8 @@ inline Work make_work(const DevPlan &pl, void *base) {
   w.status = I(); w.phase = I(); w.iter = I(); w.kvec = I(); w.nhist = I(); w.prec = I();
   w.npass32 = I();
   w.stall32 = I();
+  w.mixstep = I();
+  w.dampsw = I();
   w.efermi = D(); w.energy = D(); w.resid = D(); w.best32 = D();
   w.active = I();
   w.active_list = I();

@@ -22,6 +22,7 @@
 #include "internal.cuh"
 
 #include <cmath>
+#include <math_constants.h>
 
 namespace gbxtb {
 
@@ -201,6 +202,17 @@ __global__ void k_atoms(DevParams p, DevPlan pl, Work w, const double *__restric
   const int m = blockIdx.x;
   if (!geom_due(pl, w, m)) return;
   const MolDesc md = pl.mol[m];
+  // a molecule with a non-finite coordinate is refused here: status
+  // NONFINITE, phase Done, and no later kernel works on it
+  int bad = 0;
+  for (int k = threadIdx.x; k < 3 * md.natom; k += blockDim.x) bad |= !isfinite(pos[3 * (int64_t)md.atom0 + k]);
+  if (__syncthreads_or(bad)) {
+    if (threadIdx.x == 0) {
+      w.status[m] |= GBXTB_MOL_NONFINITE;
+      w.phase[m] = kPhaseDone;
+    }
+    return;
+  }
   const double kcn = p.g[7], cn_cut = p.g[8], rep_cut = p.g[9], kexp = p.g[6];
   for (int ia = threadIdx.x; ia < md.natom; ia += blockDim.x) {
     const int a = md.atom0 + ia;
@@ -416,7 +428,13 @@ __global__ void k_force_pairs(DevParams p, DevPlan pl, Work w, const double *__r
 __global__ void k_force_atoms(DevParams p, DevPlan pl, Work w, const double *__restrict__ pos,
                               double *__restrict__ grad_out) {
   const int m = blockIdx.x;
-  if (!force_due(pl, w, m)) return;
+  if (!force_due(pl, w, m)) {
+    // a failed molecule of a batch: its gradient is not a number
+    if (!pl.pool)
+      for (int k = threadIdx.x; k < 3 * pl.mol[m].natom; k += blockDim.x)
+        grad_out[3 * (int64_t)pl.mol[m].atom0 + k] = CUDART_NAN;
+    return;
+  }
   const MolDesc md = pl.mol[m];
   const double kcn = p.g[7], cn_cut = p.g[8], rep_cut = p.g[9], kexp = p.g[6];
   for (int ia = threadIdx.x; ia < md.natom; ia += blockDim.x) {

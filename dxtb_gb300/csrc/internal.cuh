@@ -115,6 +115,8 @@ struct Work {
   double *cn, *erep, *qat, *grad, *dedcn;  // grad: [natom][3]
   // per molecule
   int32_t *status, *phase, *iter, *kvec, *nhist;
+  int32_t *mixstep; // mixer calls made (the reference mixer's iter_step)
+  int32_t *dampsw;  // 1: damp_dynamic has switched the mixing parameter
   int32_t *prec;    // 0: the next pass runs in FP32, 1: in FP64
   int32_t *npass32; // number of FP32 passes the molecule made
   int32_t *stall32; // FP32 passes since the potential change last halved
@@ -219,16 +221,21 @@ __device__ __forceinline__ int list_mol(const Work &w, const int32_t *list, int 
   return list[idx];
 }
 
-// Geometry kernels work on every molecule of a batch, and in a pool only on
-// the molecules admitted since the last step.
+// Geometry kernels work on every molecule of a batch that has not failed
+// (non-finite positions, overlap not positive definite), and in a pool only
+// on the molecules admitted since the last step.
 __device__ __forceinline__ bool geom_due(const DevPlan &pl, const Work &w, int m) {
-  return !pl.pool || w.phase[m] == kPhaseSetup;
+  return pl.pool ? w.phase[m] == kPhaseSetup : w.phase[m] != kPhaseDone;
 }
 
-// Force kernels work on every molecule of a batch, and in a pool only on the
-// molecules that converged in this step.
+// Status bits of a molecule whose result is not a number: Fermi level not
+// found, overlap not positive definite, non-finite input or values.
+constexpr int kFailBits = GBXTB_MOL_FERMI_FAIL | GBXTB_MOL_CHOLESKY_FAIL | GBXTB_MOL_NONFINITE;
+
+// Force kernels work on every molecule of a batch that has not failed, and
+// in a pool only on the molecules that converged in this step.
 __device__ __forceinline__ bool force_due(const DevPlan &pl, const Work &w, int m) {
-  return !pl.pool || w.phase[m] == kPhaseFinished;
+  return pl.pool ? w.phase[m] == kPhaseFinished : (w.status[m] & kFailBits) == 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -243,11 +250,11 @@ int launch_cholesky(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s);
 int launch_cholesky_blocked(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s);
 void launch_fock(const DevPlan &pl, const Work &w, cudaStream_t s);
 void launch_eigensolve_tridiag(const DevPlan &pl, const Work &w, cudaStream_t s);
-void launch_fermi(const DevPlan &pl, const Work &w, double kt, int maxiter, cudaStream_t s);
+void launch_fermi(const DevPlan &pl, const Work &w, double kt, int maxiter, double thresh, cudaStream_t s);
 void launch_eigenvectors(const DevPlan &pl, const Work &w, cudaStream_t s);
 void launch_density(const DevPlan &pl, const Work &w, cudaStream_t s);
 void launch_charges_mix(const DevParams &p, const DevPlan &pl, const Work &w,
-                        const gbxtb_options &o, int iteration, cudaStream_t s);
+                        const gbxtb_options &o, cudaStream_t s);
 void launch_energies(const DevParams &p, const DevPlan &pl, const Work &w, double kt,
                      double *energy_out, double *charges_out, cudaStream_t s);
 void launch_forces(const DevParams &p, const DevPlan &pl, const Work &w, const double *pos,
@@ -258,5 +265,9 @@ void launch_forces(const DevParams &p, const DevPlan &pl, const Work &w, const d
 // the device scratch a plan's gbxtb_singlepoint needs.
 int set_error(int code, const std::string &msg);
 size_t plan_workspace_bytes(const gbxtb_plan *plan);
+// CUDA device the plan's buffers live on.
+int plan_device(const gbxtb_plan *plan);
+// GBXTB_OK, or GBXTB_ERR_ARG with a message when an SCF option is out of range.
+int check_options(const gbxtb_options *opts);
 
 }  // namespace gbxtb

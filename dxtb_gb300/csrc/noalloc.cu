@@ -10,14 +10,21 @@
 // routine.
 //
 // The array (GBXTB_NOALLOC_SCRATCH_BYTES) is a file-scope __device__
-// variable: every GPU that loads the library holds it until the process
-// exits.  In host code its name is only a host-side stand-in, not a device
-// address, so its device address is looked up with cudaGetSymbolAddress once
-// per device, with that device current, by the first call made on that
-// device; that first call should come before any stream capture.  All calls
-// share the one array and it keeps the previous call's contents (the
-// single-point driver clears every buffer it reads before use); calls whose
-// GPU work overlaps race on it.
+// variable.  In host code its name is only a host-side stand-in, not a
+// device address, so its device address is looked up with
+// cudaGetSymbolAddress once per device, with that device current, by the
+// first call made on that device.  Under CUDA's lazy module loading (the
+// default) that first lookup is also what loads this file's module onto the
+// device, so the array occupies device memory from the first call on a
+// device until the process exits; make that first call at set-up, before
+// any stream capture.  The cached address does not survive cudaDeviceReset.
+// The first call on a plan, and the first after the options or the scratch
+// address changed (a gbxtb_singlepoint call with a workspace in between),
+// also creates the plan's capture stream and instantiates its pass graphs,
+// which is driver work that can take device memory; a warm-up call at
+// set-up does it once.  All calls share the one array and it keeps the
+// previous call's contents (the single-point driver clears every buffer it
+// reads before use); calls whose GPU work overlaps race on it.
 #include "internal.cuh"
 
 #include <mutex>
@@ -53,6 +60,12 @@ extern "C" int gbxtb_singlepoint_noalloc(gbxtb_plan *plan, const gbxtb_options *
   if (e != cudaSuccess)
     return gbxtb::set_error(GBXTB_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
   if (dev < 0 || dev >= kMaxDevices) return gbxtb::set_error(GBXTB_ERR_ARG, "device ordinal out of range");
+  // the scratch is the current device's array; the plan's buffers must be
+  // on the same device
+  if (dev != gbxtb::plan_device(plan))
+    return gbxtb::set_error(GBXTB_ERR_ARG, "the current device (" + std::to_string(dev) +
+                                               ") is not the device of the plan (" +
+                                               std::to_string(gbxtb::plan_device(plan)) + ")");
   void *scratch = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_mu);

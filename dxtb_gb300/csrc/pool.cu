@@ -49,6 +49,8 @@ __global__ void k_pool_reset(DevPlan pl, Work w, const int32_t *slots, int n, in
     w.prec[m] = mixed ? 0 : 1;
     w.npass32[m] = 0;
     w.stall32[m] = 0;
+    w.mixstep[m] = 0;
+    w.dampsw[m] = 0;
     w.best32[m] = 1.0e300;
     for (int c = 0; c < 6; ++c) w.energy[(size_t)m * 6 + c] = 0.0;
   }
@@ -156,9 +158,8 @@ int gbxtb_pool_create(gbxtb_ctx *ctx, const gbxtb_options *opts, int32_t nslots,
                       int32_t cap_shells, int32_t cap_aos, gbxtb_pool **out, size_t *device_bytes) {
   if (!ctx || !opts || !out || nslots < 1 || cap_atoms < 1 || cap_shells < 1 || cap_aos < 1)
     return fail(GBXTB_ERR_ARG, "null argument or empty pool");
-  if (opts->maxiter < 0 || opts->fermi_maxiter < 1 || !(opts->kt > 0.0) || opts->broyden_memory < 1 ||
-      opts->broyden_memory > kHistMax || opts->profile)
-    return fail(GBXTB_ERR_ARG, "invalid options (profiling is not available for pools)");
+  if (const int orc = check_options(opts)) return orc;
+  if (opts->profile) return fail(GBXTB_ERR_ARG, "profiling is not available for pools");
   auto *pool = new (std::nothrow) gbxtb_pool();
   if (!pool) return fail(GBXTB_ERR_NOMEM, "host allocation failed");
   pool->opts = *opts;
@@ -455,7 +456,7 @@ int gbxtb_pool_step_launch(gbxtb_pool *pool, void *stream) {
       launch_tridiag(pl, w, plan->maxn, s);
       launch_bisect(pl, w, plan->maxn, o.kt, nullptr, pl.nmol, 256, s);
     }
-    launch_fermi(pl, w, o.kt, o.fermi_maxiter, s);
+    launch_fermi(pl, w, o.kt, o.fermi_maxiter, o.fermi_thresh, s);
     launch_invit(pl, w, plan->maxn, s);
     if (tail)
       launch_backtransform(pl, w, plan->maxn, w.active_list, active, s);
@@ -463,7 +464,7 @@ int gbxtb_pool_step_launch(gbxtb_pool *pool, void *stream) {
       launch_backtransform(pl, w, plan->maxn, nullptr, pl.nmol, s);
     launch_gemm(pl, w, plan->tile0, plan->ntile, 2, 0, s);
     launch_gemm(pl, w, plan->tile0, plan->ntile, 3, 0, s);
-    launch_charges_mix(p, pl, w, o, 0, s);
+    launch_charges_mix(p, pl, w, o, s);
     launch_count_active(pl, w, s);
     // forces of the molecules that converged in this pass (phase Finished)
     launch_gemm(pl, w, plan->tile0, plan->ntile, 4, 1, s);

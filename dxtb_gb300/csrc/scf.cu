@@ -1,5 +1,5 @@
 // SCF state update of GFN1-xTB on the device: Fermi-Dirac occupations,
-// Mulliken charges, ES2/ES3 potential, modified-Broyden mixing with the
+// Mulliken charges, ES2/ES3 potential, potential mixing with the
 // reference's convergence test, and the energy assembly.
 //
 // Reference behaviour reproduced (dxtb, src/dxtb/_src/...):
@@ -17,13 +17,28 @@
 //                 ES3 gam3 q^3/3, electronic free energy kT sum f ln f +
 //                 (1-f) ln(1-f) over both spin channels with eps clamping),
 //                 calculators/types/energy.py:148-325 (total = classical + SCF)
-// The mixer is modified Broyden (Johnson, Phys. Rev. B 38, 12807 (1988)) on
-// the shell-resolved potential with orbital-multiplicity weights, so that all
-// norms and inner products equal those of the orbital-resolved vector the
-// reference mixes; the converged fixed point does not depend on the mixer.
+// Mixers (gbxtb_options.mixer), all on the shell-resolved potential with
+// orbital-multiplicity weights, so that every norm and inner product equals
+// that of the orbital-resolved vector the reference mixes (the orbital
+// potential is the shell value repeated over the shell's 2l+1 orbitals, and
+// every mixer forms linear combinations of such vectors):
+//   Broyden    modified Broyden (Johnson, Phys. Rev. B 38, 12807 (1988)),
+//              the engine's default;
+//   Anderson   the reference's Anderson/Eyert mixer step for step
+//              (scf/mixer/anderson.py:200-317: soft start with damp_init,
+//              then `generations` differences, diagonal rescaling
+//              1 + offset^2, x_bar + damp f_bar), the mixer the reference's
+//              default full-mode SCF runs (scf/unrolling/base.py:81-99);
+//   simple     x + damp (F(x) - x) (scf/mixer/simple.py).
+// mix_guess = 0 takes the first output potential unmixed, and damp_dynamic
+// switches the mixing parameter once the potential change drops below 0.1,
+// as scf/unrolling/default.py:92-121 does.  The converged fixed point does
+// not depend on the mixer; which of several fixed points an SCF reaches
+// can.
 #include "internal.cuh"
 
 #include <cmath>
+#include <math_constants.h>
 
 namespace gbxtb {
 
@@ -34,7 +49,7 @@ constexpr double kEps = 2.220446049250313e-16;
 // ---------------------------------------------------------------------------
 // Fermi occupations; also decides how many eigenvectors are needed (kvec).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k_fermi(DevPlan pl, Work w, double kt, int maxiter) {
+__global__ void __launch_bounds__(128) k_fermi(DevPlan pl, Work w, double kt, int maxiter, double thresh) {
   const int m = blockIdx.x;
   if (w.phase[m] == kPhaseDone) return;
   const MolDesc md = pl.mol[m];
@@ -43,7 +58,7 @@ __global__ void __launch_bounds__(128) k_fermi(DevPlan pl, Work w, double kt, in
   double *occ[2] = {w.occ + md.ao0, w.occ + pl.nao + md.ao0};
   __shared__ double red[32];
   __shared__ int s_conv;
-  const double thr = sqrt(kEps);
+  const double thr = thresh > 0.0 ? thresh : sqrt(kEps);
   double ef[2], target[2];
   bool nonempty[2];
   for (int s = 0; s < 2; ++s) {
@@ -110,15 +125,10 @@ __global__ void __launch_bounds__(128) k_fermi(DevPlan pl, Work w, double kt, in
 // ---------------------------------------------------------------------------
 struct MixOpts {
   double x_atol, x_atol_max, alpha, w0, kt;
-  int maxiter, memory, iteration;
+  double damp, damp_init, offset, damp_dyn;
+  int maxiter, memory;
+  int mixer, generations, soft_start, mix_guess, damp_dynamic;
 };
-
-__device__ __forceinline__ double wdot(const double *a, const double *b, const int32_t *l, int n) {
-  // orbital-multiplicity weighted dot product; caller reduces
-  double s = 0.0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) s += (2.0 * l[i] + 1.0) * a[i] * b[i];
-  return s;
-}
 
 constexpr int kMixThreads = 256;
 // mixed precision: potential change (orbital L2 norm) below which a molecule
@@ -136,6 +146,194 @@ constexpr int kLowpMaxPasses = 1000;
 constexpr double kLowpStallBelow = 1e-3;
 constexpr int kLowpStall = 8;
 constexpr int kMaxMem = 30;
+constexpr int kHistSlots = 29;  // hist_df / hist_u slots per shell (the workspace's kHistMax)
+
+// Solve a x = b in place for a small system (n <= kMaxMem - 1, augmented
+// column n) by Gaussian elimination with partial pivoting, as LAPACK's gesv
+// (which torch.linalg.solve calls) does; one warp, result in a[.][n].
+__device__ void warp_solve(double (*a)[kMaxMem + 1], int n) {
+  const int lane = threadIdx.x & 31;
+  for (int piv = 0; piv < n; ++piv) {
+    int best = piv;
+    for (int r = piv + 1; r < n; ++r)
+      if (fabs(a[r][piv]) > fabs(a[best][piv])) best = r;
+    __syncwarp();
+    if (best != piv)
+      for (int c = lane; c <= n; c += 32) {
+        const double t = a[piv][c];
+        a[piv][c] = a[best][c];
+        a[best][c] = t;
+      }
+    __syncwarp();
+    const double inv = 1.0 / a[piv][piv];
+    for (int r = piv + 1; r < n; ++r) {
+      const double fac = a[r][piv] * inv;
+      __syncwarp();
+      for (int c = lane + piv; c <= n; c += 32) a[r][c] -= fac * a[piv][c];
+      __syncwarp();
+    }
+  }
+  // back substitution (lane 0; n is small)
+  if (lane == 0)
+    for (int r = n - 1; r >= 0; --r) {
+      double v = a[r][n];
+      for (int c = r + 1; c < n; ++c) v -= a[r][c] * a[c][n];
+      a[r][n] = v / a[r][r];
+    }
+  __syncwarp();
+}
+
+// Anderson/Eyert step of the reference (scf/mixer/anderson.py:200-317) for
+// one molecule (one block).  History: rings of generations + 1 potentials x
+// and differences F = F(x) - x in hist_u / hist_df; ring slot step % R holds
+// the current x (= vin, the previous mixed potential or the guess) and F.
+__device__ void anderson_step(const DevPlan &pl, const Work &w, const MolDesc &md, const MixOpts &o, int step,
+                              double damp, double (*a)[kMaxMem + 1]) {
+  const int nsh = md.nsh;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int32_t *lsh = pl.sh_l + md.sh0;
+  double *vin = w.vin + md.sh0;
+  const double *vout = w.vout + md.sh0;
+  const int R = o.generations + 1;
+  const int cur = step % R;
+  auto X = [&](int slot) { return w.hist_u + (size_t)slot * pl.nsh + md.sh0; };
+  auto F = [&](int slot) { return w.hist_df + (size_t)slot * pl.nsh + md.sh0; };
+  double *x0 = X(cur), *f0 = F(cur);
+  for (int i = threadIdx.x; i < nsh; i += blockDim.x) {
+    x0[i] = vin[i];
+    f0[i] = vout[i] - vin[i];
+  }
+  __syncthreads();
+  const int it = step + 1;  // the reference's iter_step after its increment
+  if (it > o.generations || (it > 1 && !o.soft_start)) {
+    const int n = min(it - 1, o.generations);
+    // a_ij = <F0 - F_i | F0 - F_j>, b_i = <F0 - F_i | F0>, i, j = 1..n
+    for (int pidx = wid; pidx < n * (n + 1); pidx += nw) {
+      const int ii = pidx / (n + 1), jj = pidx % (n + 1);
+      const double *fi = F((cur - 1 - ii + R) % R);
+      double s = 0.0;
+      if (jj < n) {
+        const double *fj = F((cur - 1 - jj + R) % R);
+        for (int t = lane; t < nsh; t += 32) s += (2.0 * lsh[t] + 1.0) * (f0[t] - fi[t]) * (f0[t] - fj[t]);
+      } else {
+        for (int t = lane; t < nsh; t += 32) s += (2.0 * lsh[t] + 1.0) * (f0[t] - fi[t]) * f0[t];
+      }
+      s = warp_sum(s);
+      if (lane == 0) a[ii][jj] = (ii == jj && o.offset >= 0.0) ? s * (1.0 + o.offset * o.offset) : s;
+    }
+    __syncthreads();
+    if (wid == 0) warp_solve(a, n);
+    __syncthreads();
+    // x_bar = x0 + sum_i theta_i (x_i - x0), f_bar = F0 + sum_i theta_i (F_i - F0)
+    double *xn = X((cur + 1) % R);
+    for (int t = threadIdx.x; t < nsh; t += blockDim.x) {
+      double xb = 0.0, fb = 0.0;
+      for (int i = 0; i < n; ++i) {
+        const int sl = (cur - 1 - i + R) % R;
+        const double th = a[i][n];
+        xb += th * (X(sl)[t] - x0[t]);
+        fb += th * -(f0[t] - F(sl)[t]);
+      }
+      xb += x0[t];
+      fb += f0[t];
+      const double xm = xb + damp * fb;
+      xn[t] = xm;
+      vin[t] = xm;
+    }
+  } else {
+    double *xn = X((cur + 1) % R);
+    for (int t = threadIdx.x; t < nsh; t += blockDim.x) {
+      const double xm = x0[t] + f0[t] * o.damp_init;
+      xn[t] = xm;
+      vin[t] = xm;
+    }
+  }
+}
+
+// Modified Broyden step (Johnson 1988) with step alpha, unit weights and
+// w0: the engine's default mixer.  `step` counts earlier calls: the first
+// call only records x and F.
+__device__ void broyden_step(const DevPlan &pl, const Work &w, const MolDesc &md, int m, const MixOpts &o,
+                             int step, double (*a)[kMaxMem + 1]) {
+  const int nsh = md.nsh;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int32_t *lsh = pl.sh_l + md.sh0;
+  double *vin = w.vin + md.sh0;
+  const double *vout = w.vout + md.sh0;
+  double *xprev = w.xprev + md.sh0, *fprev = w.fprev + md.sh0;
+  __shared__ double red[32];
+  const int mem = o.memory;
+  if (step == 0) {
+    for (int i = threadIdx.x; i < nsh; i += blockDim.x) {
+      const double f = vout[i] - vin[i];
+      xprev[i] = vin[i];
+      fprev[i] = f;
+      vin[i] = vin[i] + o.alpha * f;
+    }
+    return;
+  }
+  const int nst = w.nhist[m];  // number of stored (dF, u) pairs ever pushed
+  // new difference pair
+  double nrm = 0.0;
+  for (int i = threadIdx.x; i < nsh; i += blockDim.x) {
+    const double df = (vout[i] - vin[i]) - fprev[i];
+    nrm += (2.0 * lsh[i] + 1.0) * df * df;
+  }
+  nrm = sqrt(block_sum(nrm, red));
+  const double inrm = (nrm > 0.0) ? 1.0 / nrm : 0.0;
+  const int slot = nst % mem;
+  double *DF = w.hist_df + (size_t)slot * pl.nsh + md.sh0;
+  double *U = w.hist_u + (size_t)slot * pl.nsh + md.sh0;
+  for (int i = threadIdx.x; i < nsh; i += blockDim.x) {
+    const double f = vout[i] - vin[i];
+    const double df = (f - fprev[i]) * inrm;
+    DF[i] = df;
+    U[i] = o.alpha * df + (vin[i] - xprev[i]) * inrm;
+  }
+  __syncthreads();
+  const int k = min(nst + 1, mem);
+  // Gram matrix a_ij = <dF_i, dF_j> + w0^2 delta_ij and rhs c_i = <dF_i, F>
+  for (int pidx = wid; pidx < k * (k + 1); pidx += nw) {
+    const int ii = pidx / (k + 1), jj = pidx % (k + 1);
+    const double *x = w.hist_df + (size_t)ii * pl.nsh + md.sh0;
+    double s = 0.0;
+    if (jj < k) {
+      const double *y = w.hist_df + (size_t)jj * pl.nsh + md.sh0;
+      for (int t = lane; t < nsh; t += 32) s += (2.0 * lsh[t] + 1.0) * x[t] * y[t];
+    } else {
+      for (int t = lane; t < nsh; t += 32) s += (2.0 * lsh[t] + 1.0) * x[t] * (vout[t] - vin[t]);
+    }
+    s = warp_sum(s);
+    if (lane == 0) a[ii][jj] = s + ((ii == jj && jj < k) ? o.w0 * o.w0 : 0.0);
+  }
+  __syncthreads();
+  // Gauss-Jordan elimination (matrix is symmetric positive definite)
+  if (wid == 0) {
+    for (int piv = 0; piv < k; ++piv) {
+      const double inv = 1.0 / a[piv][piv];
+      __syncwarp();
+      for (int c = lane; c <= k; c += 32) a[piv][c] *= inv;
+      __syncwarp();
+      for (int r = 0; r < k; ++r) {
+        if (r == piv) continue;
+        const double fac = a[r][piv];
+        __syncwarp();
+        for (int c = lane; c <= k; c += 32) a[r][c] -= fac * a[piv][c];
+        __syncwarp();
+      }
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nsh; i += blockDim.x) {
+    const double f = vout[i] - vin[i];
+    double corr = 0.0;
+    for (int t = 0; t < k; ++t) corr += a[t][k] * w.hist_u[(size_t)t * pl.nsh + md.sh0 + i];
+    xprev[i] = vin[i];
+    fprev[i] = f;
+    vin[i] = vin[i] + o.alpha * f - corr;
+  }
+  if (threadIdx.x == 0) w.nhist[m] = nst + 1;
+}
 
 __global__ void __launch_bounds__(kMixThreads) k_charges_mix(DevParams p, DevPlan pl, Work w, MixOpts o) {
   const int m = blockIdx.x;
@@ -294,79 +492,27 @@ __global__ void __launch_bounds__(kMixThreads) k_charges_mix(DevParams p, DevPla
     return;
   }
 
-  // 5. modified Broyden step
-  double *xprev = w.xprev + md.sh0, *fprev = w.fprev + md.sh0;
-  const int mem = o.memory;
-  const int nst = w.nhist[m];  // number of stored (dF, u) pairs ever pushed
-  if (iter == 0) {
-    for (int i = threadIdx.x; i < nsh; i += blockDim.x) {
-      const double f = vout[i] - vin[i];
-      xprev[i] = vin[i];
-      fprev[i] = f;
-      vin[i] = vin[i] + o.alpha * f;
-    }
+  // 5. mixing.  The first output potential is taken unmixed without
+  // mix_guess (scf/unrolling/default.py:92-96); the mixer starts at the
+  // next pass.
+  if (iter == 0 && !o.mix_guess) {
+    for (int i = threadIdx.x; i < nsh; i += blockDim.x) vin[i] = vout[i];
     return;
   }
-  // new difference pair
-  double nrm = 0.0;
-  for (int i = threadIdx.x; i < nsh; i += blockDim.x) {
-    const double df = (vout[i] - vin[i]) - fprev[i];
-    nrm += (2.0 * lsh[i] + 1.0) * df * df;
+  const int step = w.mixstep[m];  // mixer calls before this one
+  const double damp = w.dampsw[m] ? o.damp_dyn : o.damp;
+  if (o.mixer == GBXTB_MIXER_ANDERSON) {
+    anderson_step(pl, w, md, o, step, damp, a);
+  } else if (o.mixer == GBXTB_MIXER_SIMPLE) {
+    for (int i = threadIdx.x; i < nsh; i += blockDim.x) vin[i] = vin[i] + (vout[i] - vin[i]) * damp;
+  } else {
+    broyden_step(pl, w, md, m, o, step, a);
   }
-  nrm = sqrt(block_sum(nrm, red));
-  const double inrm = (nrm > 0.0) ? 1.0 / nrm : 0.0;
-  const int slot = nst % mem;
-  double *DF = w.hist_df + (size_t)slot * pl.nsh + md.sh0;
-  double *U = w.hist_u + (size_t)slot * pl.nsh + md.sh0;
-  for (int i = threadIdx.x; i < nsh; i += blockDim.x) {
-    const double f = vout[i] - vin[i];
-    const double df = (f - fprev[i]) * inrm;
-    DF[i] = df;
-    U[i] = o.alpha * df + (vin[i] - xprev[i]) * inrm;
+  if (threadIdx.x == 0) {
+    w.mixstep[m] = step + 1;
+    // the reference switches after the step, for the steps that follow
+    if (o.damp_dynamic && l2 < 0.1) w.dampsw[m] = 1;
   }
-  __syncthreads();
-  const int k = min(nst + 1, mem);
-  // Gram matrix a_ij = <dF_i, dF_j> + w0^2 delta_ij and rhs c_i = <dF_i, F>
-  for (int pidx = wid; pidx < k * (k + 1); pidx += nw) {
-    const int ii = pidx / (k + 1), jj = pidx % (k + 1);
-    const double *x = w.hist_df + (size_t)ii * pl.nsh + md.sh0;
-    double s = 0.0;
-    if (jj < k) {
-      const double *y = w.hist_df + (size_t)jj * pl.nsh + md.sh0;
-      for (int t = lane; t < nsh; t += 32) s += (2.0 * lsh[t] + 1.0) * x[t] * y[t];
-    } else {
-      for (int t = lane; t < nsh; t += 32) s += (2.0 * lsh[t] + 1.0) * x[t] * (vout[t] - vin[t]);
-    }
-    s = warp_sum(s);
-    if (lane == 0) a[ii][jj] = s + ((ii == jj && jj < k) ? o.w0 * o.w0 : 0.0);
-  }
-  __syncthreads();
-  // Gauss-Jordan elimination (matrix is symmetric positive definite)
-  if (wid == 0) {
-    for (int piv = 0; piv < k; ++piv) {
-      const double inv = 1.0 / a[piv][piv];
-      __syncwarp();
-      for (int c = lane; c <= k; c += 32) a[piv][c] *= inv;
-      __syncwarp();
-      for (int r = 0; r < k; ++r) {
-        if (r == piv) continue;
-        const double fac = a[r][piv];
-        __syncwarp();
-        for (int c = lane; c <= k; c += 32) a[r][c] -= fac * a[piv][c];
-        __syncwarp();
-      }
-    }
-  }
-  __syncthreads();
-  for (int i = threadIdx.x; i < nsh; i += blockDim.x) {
-    const double f = vout[i] - vin[i];
-    double corr = 0.0;
-    for (int t = 0; t < k; ++t) corr += a[t][k] * w.hist_u[(size_t)t * pl.nsh + md.sh0 + i];
-    xprev[i] = vin[i];
-    fprev[i] = f;
-    vin[i] = vin[i] + o.alpha * f - corr;
-  }
-  if (threadIdx.x == 0) w.nhist[m] = nst + 1;
 }
 
 // Count and list (in index order) the molecules that still iterate, and
@@ -407,10 +553,13 @@ __global__ void k_count_active(DevPlan pl, Work w) {
   }
 }
 
+// Energies and atomic charges; those of failed molecules (kFailBits) are
+// not a number.
 __global__ void k_outputs(DevPlan pl, Work w, double *energy_out, double *charges_out) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < pl.nmol && energy_out) energy_out[t] = w.energy[t * 6];
-  if (t < pl.natom && charges_out) charges_out[t] = w.qat[t];
+  if (t < pl.nmol && energy_out) energy_out[t] = (w.status[t] & kFailBits) ? CUDART_NAN : w.energy[t * 6];
+  if (t < pl.natom && charges_out)
+    charges_out[t] = (w.status[pl.atom_mol[t]] & kFailBits) ? CUDART_NAN : w.qat[t];
 }
 
 }  // namespace
@@ -419,12 +568,12 @@ void launch_count_active(const DevPlan &pl, const Work &w, cudaStream_t s) {
   k_count_active<<<1, 256, 0, s>>>(pl, w);
 }
 
-void launch_fermi(const DevPlan &pl, const Work &w, double kt, int maxiter, cudaStream_t s) {
-  k_fermi<<<pl.nmol, 128, 0, s>>>(pl, w, kt, maxiter);
+void launch_fermi(const DevPlan &pl, const Work &w, double kt, int maxiter, double thresh, cudaStream_t s) {
+  k_fermi<<<pl.nmol, 128, 0, s>>>(pl, w, kt, maxiter, thresh);
 }
 
 void launch_charges_mix(const DevParams &p, const DevPlan &pl, const Work &w,
-                        const gbxtb_options &o, int iteration, cudaStream_t s) {
+                        const gbxtb_options &o, cudaStream_t s) {
   MixOpts mo;
   mo.x_atol = o.x_atol;
   mo.x_atol_max = o.x_atol_max;
@@ -433,7 +582,15 @@ void launch_charges_mix(const DevParams &p, const DevPlan &pl, const Work &w,
   mo.kt = o.kt;
   mo.maxiter = o.maxiter;
   mo.memory = o.broyden_memory < 1 ? 1 : (o.broyden_memory > kMaxMem - 1 ? kMaxMem - 1 : o.broyden_memory);
-  mo.iteration = iteration;
+  mo.mixer = o.mixer;
+  mo.generations = o.generations < 1 ? 1 : (o.generations > kHistSlots - 1 ? kHistSlots - 1 : o.generations);
+  mo.damp = o.damp;
+  mo.damp_init = o.damp_init;
+  mo.offset = o.diagonal_offset;
+  mo.damp_dyn = o.damp_dynamic_factor;
+  mo.soft_start = o.soft_start;
+  mo.mix_guess = o.mix_guess;
+  mo.damp_dynamic = o.damp_dynamic;
   k_charges_mix<<<pl.nmol, kMixThreads, 0, s>>>(p, pl, w, mo);
 }
 

@@ -88,4 +88,6 @@ def main(src: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/src")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python -m dxtb_gb300.data.make_params /path/to/dxtb/src")
+    main(sys.argv[1])

@@ -29,7 +29,7 @@ import numpy as np
 import torch
 
 from . import _lib, params
-from .calculator import DEFAULT_OPTS, _Context
+from .calculator import _Context, engine_options, resolve_opts
 
 __all__ = ["Server", "Request", "size_class_capacity"]
 
@@ -172,22 +172,10 @@ class Server:
         if device is None:
             device = torch.cuda.current_device()
         self.device = device
-        o = dict(DEFAULT_OPTS)
-        o.update(opts or {})
-        excl = set(o.get("exclude", []))
-        if "disp" not in excl:
-            raise ValueError("D3 dispersion is not available; pass opts={'exclude': ['disp']}")
-        opt = _lib.Options()
-        opt.maxiter = int(o["maxiter"])
-        opt.fermi_maxiter = int(o["fermi_maxiter"])
-        opt.broyden_memory = int(o["broyden_memory"])
-        opt.want_forces = 1
-        opt.x_atol = float(o["x_atol"])
-        opt.x_atol_max = float(o["x_atol_max"])
-        opt.kt = float(o["fermi_etemp"]) * params.KELVIN2AU
-        opt.broyden_alpha = float(o["broyden_alpha"])
-        opt.profile = 0
-        opt.mixed_precision = 1 if o.get("mixed_precision", True) else 0
+        o = resolve_opts(opts)
+        if o["profile"]:
+            raise ValueError("profiling is not available for served requests")
+        opt = engine_options(o, forces=True)
         self.opts = o
         ctx = _Context.get(device)
         self.pools: list[_Pool] = []

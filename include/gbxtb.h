@@ -11,7 +11,8 @@
  * src/dxtb/_src/calculators/types/autograd.py:82-201 and
  * src/dxtb/_src/calculators/types/analytical.py:63-222 for the forces).
  * A Python (ctypes) binding that mirrors dxtb's GFN1Calculator sits in
- * dxtb_gb300/calculator.py; INTEGRATION.md shows the binding.
+ * dxtb_gb300/calculator.py, and dxtb_gb300/csrc/torch_ops.cpp exposes the
+ * single point and its adjoint as torch operators (torch.ops.gbxtb.*).
  */
 #ifndef GBXTB_H
 #define GBXTB_H
@@ -80,23 +81,56 @@ typedef struct {
   const double *globals;      /* [GBXTB_GLOBALS] */
 } gbxtb_params;
 
-/* SCF options (dxtb: calculators/config/scf.py:32-433; defaults.py:130-260). */
+/* SCF mixers (gbxtb_options.mixer). */
+#define GBXTB_MIXER_BROYDEN 0  /* modified Broyden (Johnson 1988): the engine's default */
+#define GBXTB_MIXER_ANDERSON 1 /* the reference's Anderson/Eyert mixer, step for step
+                                  (scf/mixer/anderson.py:200-317): the mixer its
+                                  default full-mode SCF runs (scf/unrolling/base.py:81-99) */
+#define GBXTB_MIXER_SIMPLE 2   /* linear mixing x + damp (F(x) - x) (scf/mixer/simple.py) */
+
+/* SCF options (dxtb: calculators/config/scf.py:32-433; defaults.py:130-260).
+ * gbxtb_default_options() fills every field with the reference's defaults. */
 typedef struct {
   int32_t maxiter;        /* SCF iterations (reference option "maxiter") */
   int32_t fermi_maxiter;  /* Newton steps for the Fermi level (200) */
-  int32_t broyden_memory; /* mixer history length */
+  int32_t broyden_memory; /* Broyden history length (1..29) */
   int32_t want_forces;    /* 0: energy only; 1: energy and forces */
   double x_atol;          /* L2 norm of the potential change ("x_atol") */
   double x_atol_max;      /* max norm of the potential change ("x_atol_max") */
   double kt;              /* electronic temperature in Hartree (fermi_etemp * k_B) */
-  double broyden_alpha;   /* mixer step */
+  double broyden_alpha;   /* Broyden step */
   int32_t profile;        /* 1: time each kernel class with CUDA events (gbxtb_get_profile) */
   int32_t mixed_precision; /* 1: SCF passes run their linear algebra in FP32 while the
                               potential change is above 1e-4 and still falling
                               (8 passes without halving below 1e-3 end them);
                               convergence and the final state are always FP64.
                               0: every pass in FP64 */
+  int32_t mixer;           /* GBXTB_MIXER_* */
+  int32_t generations;     /* Anderson history ("damp_generations", 5; 1..28) */
+  double damp;             /* Anderson / simple mixing parameter ("damp", 0.5) */
+  double damp_init;        /* Anderson soft-start parameter ("damp_init", 0.1) */
+  double diagonal_offset;  /* Anderson diagonal rescaling ("damp_diagonal_offset",
+                              0.01); negative: no rescaling (the reference's None) */
+  int32_t soft_start;      /* Anderson: simple mixing for the first `generations`
+                              steps ("damp_soft_start", 1) */
+  int32_t mix_guess;       /* 1: the first potential is mixed with the guess
+                              ("mix_guess", 1); 0: taken unmixed
+                              (scf/unrolling/default.py:92-96) */
+  int32_t damp_dynamic;    /* 1: once the potential change is below 0.1, later
+                              steps use damp_dynamic_factor ("damp_dynamic", 0) */
+  int32_t reserved;        /* 0 */
+  double damp_dynamic_factor; /* ("damp_dynamic_factor", 0.99) */
+  double fermi_thresh;     /* |sum f - n| at which the Fermi-level Newton search
+                              stops ("fermi_thresh"); <= 0: sqrt(machine eps),
+                              the reference's default (wavefunction/filling.py:
+                              269-366) */
 } gbxtb_options;
+
+/* The reference's default SCF options (calculators/config/scf.py:139-190,
+ * constants/defaults.py): maxiter 100, x_atol 1e-4, x_atol_max 1e-5, 300 K,
+ * Anderson with damp 0.5, damp_init 0.1, 5 generations, offset 0.01, soft
+ * start, mixed guess.  Mixed precision, profiling and forces are off. */
+GBXTB_API void gbxtb_default_options(gbxtb_options *opts);
 
 /* Kernel classes reported by gbxtb_get_profile. */
 #define GBXTB_PROF_ATOMS 0        /* coordination numbers, repulsion */
@@ -159,6 +193,16 @@ GBXTB_API int gbxtb_singlepoint(gbxtb_plan *plan, const gbxtb_options *opts,
                       double *charges_dev, double *gradient_dev,
                       void *workspace_dev, size_t workspace_bytes,
                       void *stream);
+
+/* Energy gradient dE/dR ([natoms][3]) of the final state of the plan's last
+ * gbxtb_singlepoint, which must have run on the same positions and the same
+ * workspace, untouched since.  Gives the same gradient as that call with
+ * opts->want_forces = 1, so a caller that asked for the energy first gets
+ * the forces without a second SCF (the reference serves get_forces after
+ * get_energy from its cache: calculators/types/decorators.py:228-275,
+ * types/autograd.py:82-201). */
+GBXTB_API int gbxtb_forces(gbxtb_plan *plan, const double *positions_dev, double *gradient_dev,
+                           void *workspace_dev, size_t workspace_bytes, void *stream);
 
 /* Autotune the launch shapes of the eigensolver kernels for this plan on
  * real data: sets up the geometry of `positions_dev`, forms the first
@@ -266,15 +310,24 @@ GBXTB_API int gbxtb_pool_result(gbxtb_pool *pool, int32_t slot, double *energy, 
  * framework whose memory pool must not grow once it is set up, a real-time
  * loop that forbids cudaMalloc after start-up, or a plugin callback that is
  * given only a stream.  This entry point takes no workspace.  Its scratch is
- * a fixed device array of GBXTB_NOALLOC_SCRATCH_BYTES inside the library,
- * which every GPU that loads the library holds until the process exits.  It
- * calls no cudaMalloc, cudaFree or allocating library routine.  The caller
- * still owns the positions and outputs (same meaning as gbxtb_singlepoint).
- * Limits and rules:
+ * a fixed device array of GBXTB_NOALLOC_SCRATCH_BYTES inside the library.
+ * It calls no cudaMalloc, cudaFree or allocating library routine.  The
+ * caller still owns the positions and outputs (same meaning as
+ * gbxtb_singlepoint).  Limits and rules:
  *   - plans whose workspace_bytes (gbxtb_plan_create) exceed the array are
- *     rejected with GBXTB_ERR_WORKSPACE; opts->profile must be 0;
+ *     rejected with GBXTB_ERR_WORKSPACE; opts->profile must be 0; the
+ *     current device must be the plan's (else GBXTB_ERR_ARG);
  *   - the first call on a device looks up the array's device address (with
- *     that device current); make that first call before any stream capture;
+ *     that device current); under CUDA's lazy module loading this is also
+ *     when the array is loaded onto the device, which holds it from then
+ *     until the process exits.  The looked-up address does not survive
+ *     cudaDeviceReset;
+ *   - the first call on a plan, and the first after its options or scratch
+ *     address changed (e.g. a gbxtb_singlepoint call with a workspace in
+ *     between), creates the plan's capture stream and instantiates its
+ *     pass graphs: driver work that can take device memory.  Make one
+ *     warm-up call per plan and options at set-up, before any stream
+ *     capture; later calls with the same plan and options do none of this;
  *   - all calls share the one array, which keeps the last call's contents
  *     (the driver clears what it reads first): calls whose GPU work overlaps,
  *     on other streams or threads, race on it and must be serialised. */

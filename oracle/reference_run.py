@@ -21,7 +21,10 @@ import sys
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
-REFERENCE_SRC = Path(os.environ.get("DXTB_REFERENCE_SRC", "/root/reference/src"))
+# The reference's source tree: $DXTB_REFERENCE_SRC, else a `reference/src`
+# directory beside the repository's directory.
+REFERENCE_SRC = Path(os.environ.get("DXTB_REFERENCE_SRC",
+                                    Path(__file__).resolve().parents[2] / "reference" / "src"))
 REFERENCE_ROOT = REFERENCE_SRC.parent
 
 

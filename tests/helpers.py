@@ -29,3 +29,50 @@ def same_state(e1: float, e2: float) -> bool:
     energies agree far better than the gap between distinct solutions
     (distinct solutions of the synthetic molecules differ by >1e-4 Eh)."""
     return abs(e1 - e2) < 1e-5
+
+
+def restart_energy(numbers, positions, v_orbital):
+    """Oracle SCF (the engine's Broyden loop in numpy) restarted from an
+    orbital potential: (converged, iterations, energy).  A state that is a
+    fixed point of the reference's equations converges at once and keeps
+    its energy."""
+    from oracle import gfn1_oracle as go
+
+    r = go.singlepoint(numbers, positions, mixer="broyden", v_init=v_orbital, forces=False, maxiter=30)
+    return bool(r.converged), int(r.iterations), float(r.energy)
+
+
+def fd_force_component(numbers, positions, atom, axis, h=5e-4):
+    """Five-point central difference (truncation error O(h^4)) of the oracle
+    energy: the force component -dE/dR[atom, axis].  The electron count is
+    solved to 1e-13, since at the reference's sqrt(eps) Fermi tolerance the
+    energy carries ~5e-9 Eh of noise (5e-6 Eh/bohr after dividing by h)."""
+    from oracle import gfn1_oracle as go
+
+    e = {}
+    for st in (-2, -1, 1, 2):
+        p = np.array(positions, dtype=np.float64, copy=True)
+        p[atom, axis] += st * h
+        e[st] = go.singlepoint(numbers, p, mixer="broyden", forces=False, fermi_thr=1e-13).energy
+    return -(8.0 * (e[1] - e[-1]) - (e[2] - e[-2])) / (12.0 * h)
+
+
+def _star(args):
+    fn, a = args
+    return fn(*a)
+
+
+def oracle_map(fn, jobs):
+    """Run oracle jobs on all host cores (spawned workers, one BLAS thread
+    each; spawned, so that no worker inherits the parent's CUDA context)."""
+    import multiprocessing as mp
+    import os
+
+    jobs = list(jobs)
+    if len(jobs) <= 1:
+        return [fn(*a) for a in jobs]
+    for var in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+        os.environ.setdefault(var, "1")
+    nproc = min(len(jobs), os.cpu_count() or 1)
+    with mp.get_context("spawn").Pool(nproc) as pool:
+        return pool.map(_star, [(fn, a) for a in jobs], chunksize=1)

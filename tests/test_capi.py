@@ -70,6 +70,7 @@ def test_null_arguments_of_every_entry_point(lib):
         "gbxtb_pool_admit": lambda: lib.gbxtb_pool_admit(None, 1, None, None, 0.0, -1, C.byref(i32)),
         "gbxtb_pool_step_launch": lambda: lib.gbxtb_pool_step_launch(None, None),
         "gbxtb_pool_result": lambda: lib.gbxtb_pool_result(None, 0, None, None, None, None, None),
+        "gbxtb_forces": lambda: lib.gbxtb_forces(None, None, None, None, 0, None),
     }
     for name, call in calls.items():
         assert call() == _lib.GBXTB_OK - 1, name
@@ -85,3 +86,41 @@ def test_missing_library_fails_loudly(monkeypatch, tmp_path):
     monkeypatch.setattr(_lib, "LIB_PATH", tmp_path / "libgbxtb.so")
     with pytest.raises(_lib.GbxtbError, match="no CPU fallback"):
         _lib.load()
+
+
+def test_default_options_are_the_references(lib):
+    """gbxtb_default_options: the reference's SCF defaults
+    (constants/defaults.py, calculators/config/scf.py) with its Anderson
+    mixer; the engine-only switches are off."""
+    from dxtb_gb300 import _lib, params
+
+    o = _lib.default_options()
+    assert (o.maxiter, o.fermi_maxiter, o.want_forces, o.profile, o.mixed_precision) == (100, 200, 0, 0, 0)
+    assert (o.x_atol, o.x_atol_max) == (1e-4, 1e-5)
+    assert abs(o.kt - 300.0 * params.KELVIN2AU) < 1e-15
+    assert o.mixer == _lib.MIXER_ANDERSON
+    assert (o.generations, o.damp, o.damp_init, o.diagonal_offset) == (5, 0.5, 0.1, 0.01)
+    assert (o.soft_start, o.mix_guess, o.damp_dynamic, o.damp_dynamic_factor) == (1, 1, 0, 0.99)
+    assert o.fermi_thresh == 0.0
+
+
+def test_invalid_options_are_refused_before_any_device_call(lib):
+    """Out-of-range options fail with GBXTB_ERR_ARG and a message (the plan
+    pointer is checked after the options, so no device is touched)."""
+    from dxtb_gb300 import _lib
+
+    e = C.c_double()
+    bad = []
+    for field, value in (("mixer", 7), ("generations", 0), ("generations", 29), ("broyden_memory", 0),
+                         ("fermi_maxiter", 0), ("kt", 0.0), ("damp", float("nan")),
+                         ("fermi_thresh", float("inf"))):
+        o = _lib.default_options()
+        if field == "broyden_memory":
+            o.mixer = _lib.MIXER_BROYDEN
+        if field == "damp":
+            o.mixer = _lib.MIXER_SIMPLE
+        setattr(o, field, value)
+        rc = lib.gbxtb_singlepoint(C.c_void_p(1), C.byref(o), None, C.byref(e), None, None, None, 0, None)
+        bad.append((field, rc, lib.gbxtb_last_error()))
+    for field, rc, msg in bad:
+        assert rc == -1 and msg, field

@@ -63,25 +63,24 @@ def test_reference_molecules(mol):
 
 
 def test_synthetic_molecules_against_reference():
+    """The synthetic golden molecules with the reference's own mixer
+    (Anderson, every pass in FP64): every molecule ends in the reference's
+    state, energies 1e-8 Eh, charges 1e-7 e, forces 1e-6 Eh/bohr."""
     mols = load_golden("synthetic.npz")
     num, pos = pad([(m["numbers"], m["positions"]) for m in mols])
-    calc = calc_for(num)
+    calc = calc_for(num, mixer="anderson", mixed_precision=False)
     res = calc.singlepoint(torch.tensor(pos, device="cuda"), forces=True)
     e = res.energy.cpu().numpy()
     f = -res.gradient.cpu().numpy()
     q = res.charges.cpu().numpy()
-    agree = 0
     off = 0
     for k, m in enumerate(mols):
         n = len(m["numbers"])
-        assert res.status[k] == 0
-        if same_state(e[k], m["energy"]):
-            assert abs(e[k] - m["energy"]) < E_TOL, m["name"]
-            assert np.abs(q[off:off + n] - m["charges"]).max() < Q_TOL, m["name"]
-            assert np.abs(f[off:off + n] - m["forces"]).max() < F_TOL, m["name"]
-            agree += 1
+        assert res.status[k] == 0, m["name"]
+        assert abs(e[k] - m["energy"]) < E_TOL, m["name"]
+        assert np.abs(q[off:off + n] - m["charges"]).max() < Q_TOL, m["name"]
+        assert np.abs(f[off:off + n] - m["forces"]).max() < F_TOL, m["name"]
         off += n
-    assert agree >= len(mols) - 2
 
 
 def test_engine_replays_oracle_broyden():
@@ -95,6 +94,95 @@ def test_engine_replays_oracle_broyden():
         assert abs(res.energy.item() - r.energy) < 1e-10
         assert np.abs(-res.gradient.cpu().numpy() - r.forces).max() < 1e-8
         assert abs(int(res.iterations[0]) - r.iterations) <= 2
+
+
+def test_engine_replays_oracle_anderson():
+    """The device Anderson mixer is the reference's (scf/mixer/anderson.py:
+    200-317): with every pass in FP64 the engine and the oracle's restatement
+    of the reference loop take the same number of SCF iterations and agree
+    to 1e-10 Eh, in a batch of molecules of different sizes."""
+    mols = molgen.c2_batch(12)[2:10]
+    num, pos = pad(mols)
+    calc = calc_for(num, mixer="anderson", mixed_precision=False)
+    res = calc.singlepoint(torch.tensor(pos, device="cuda"), forces=True)
+    for k, (n1, p1) in enumerate(mols):
+        r = go.singlepoint(n1, p1, mixer="anderson", forces=False)
+        if not r.converged:
+            assert res.status[k] & 1
+            continue
+        assert res.status[k] == 0
+        assert abs(res.energy[k].item() - r.energy) < 1e-10, k
+        assert abs(int(res.iterations[k]) - r.iterations) <= 1, (k, int(res.iterations[k]), r.iterations)
+
+
+def test_simple_mixer_and_options():
+    """The simple mixer and the reference's mixing switches (mix_guess,
+    damp_dynamic, soft start off) change the path, not the fixed point."""
+    num, pos = molgen.c1_single()[0]
+    p = torch.tensor(pos, device="cuda")
+    e0 = calc_for(num).singlepoint(p).energy.item()
+    for extra in ({"mixer": "simple", "damp": 0.4, "maxiter": 1000},
+                  {"mixer": "anderson", "mix_guess": False},
+                  {"mixer": "anderson", "damp_dynamic": True, "damp_soft_start": False},
+                  {"mixer": "anderson", "damp_generations": 8, "damp_diagonal_offset": None}):
+        res = calc_for(num, **extra).singlepoint(p)
+        assert res.status[0] == 0, extra
+        assert abs(res.energy.item() - e0) < 1e-10, extra
+
+
+def test_torch_ops_direct():
+    """torch.ops.gbxtb.singlepoint on a plan and forces_backward, and
+    torch.autograd.grad through the calculator (which runs both), against
+    the oracle."""
+    from dxtb_gb300 import calculator as cm
+
+    mols = molgen.c3_forces(3)
+    num, pos = pad(mols)
+    calc = calc_for(num, mixed_precision=False)
+    plan = calc._plan(0, None)
+    ops = cm._ops()
+    iopts, fopts = cm._pack_options(calc._options(True))
+    rpos = calc._ragged_positions(torch.tensor(pos, device="cuda"))
+    e, q, state, st = ops.singlepoint(plan.handle.value, rpos, plan.workspace(), iopts, fopts)
+    assert st.device.type == "cpu" and (st[:, 0] == 0).all()
+    ge = torch.tensor([1.0, -2.0, 0.5], dtype=torch.float64, device="cuda")
+    g = ops.forces_backward(state, ge, plan.atom_mol)
+    off = np.concatenate([[0], np.cumsum([len(m[0]) for m in mols])])
+    for k, (n1, p1) in enumerate(mols):
+        r = go.singlepoint(n1, p1, mixer="broyden")
+        assert abs(e[k].item() - r.energy) < 1e-10
+        a, b = off[k], off[k + 1]
+        assert np.abs(-state[a:b].cpu().numpy() - r.forces).max() < 1e-8
+        assert torch.equal(g[a:b], ge[k] * state[a:b])
+    # autograd through the operators, padded layout
+    p = torch.tensor(pos, device="cuda", requires_grad=True)
+    energy = calc.get_energy(p)
+    (grad,) = torch.autograd.grad((energy * ge).sum(), p)
+    for k, (n1, p1) in enumerate(mols):
+        r = go.singlepoint(n1, p1, mixer="broyden")
+        assert np.abs(grad[k, :len(n1)].cpu().numpy() + ge[k].item() * r.forces).max() < 1e-8
+        assert (grad[k, len(n1):] == 0).all()
+
+
+def test_forces_after_energy_reuse_the_scf():
+    """get_forces after get_energy on the same positions computes the forces
+    from the converged state of that call (gbxtb_forces), with no second
+    SCF, and equals a fresh get_forces."""
+    mols = molgen.c3_forces(2)
+    num, pos = pad(mols)
+    calc = calc_for(num)
+    p = torch.tensor(pos, device="cuda")
+    calc.get_energy(p)
+    plan = calc._plan(0, None)
+    runs = plan.runs
+    f = calc.get_forces(p)
+    assert plan.runs == runs
+    fresh = calc_for(num).get_forces(p)
+    assert torch.allclose(f, fresh, atol=1e-12, rtol=0)
+    # other positions: a new SCF
+    p2 = p + 0.01
+    calc.get_energy(p2)
+    assert plan.runs == runs + 1
 
 
 def test_orbital_charges():
@@ -153,29 +241,30 @@ def test_autograd_matches_forces():
 
 
 def test_finite_differences():
-    """Central differences (h = 1e-4 bohr) on 8 random atoms of a perturbed
-    30-60-atom molecule, all displaced geometries in one batched call."""
-    num, pos = molgen.c3_forces(1)[0]
-    calc = calc_for(num)
-    f = calc.get_forces(torch.tensor(pos, device="cuda")).cpu().numpy()
-    rng = np.random.default_rng(7)
-    atoms = rng.choice(len(num), size=8, replace=False)
+    """Central differences (h = 1e-4 bohr) on 8 random atoms of each of four
+    perturbed 30-60-atom molecules, every displaced geometry in one batched
+    call, within 1e-6 Eh/bohr of the analytic forces.  The electron count is
+    solved to 1e-13 (fermi_thresh), since at the default sqrt(eps) the
+    energy carries ~1e-8 Eh of noise, 1e-4 Eh/bohr after dividing by h."""
+    fine = {"fermi_thresh": 1e-13, "x_atol": 1e-12, "x_atol_max": 1e-12, "mixed_precision": False}
     h = 1e-4
-    geoms = []
-    for a in atoms:
-        for x in range(3):
-            for sgn in (1.0, -1.0):
-                p = pos.copy()
-                p[a, x] += sgn * h
-                geoms.append(p)
-    nb = np.broadcast_to(num, (len(geoms), len(num))).copy()
-    calc_b = calc_for(nb)
-    e = calc_b.get_energy(torch.tensor(np.array(geoms), device="cuda")).cpu().numpy()
+    rng = np.random.default_rng(7)
+    geoms, nums, an = [], [], []
+    for num, pos in molgen.c3_forces(4):
+        f = calc_for(num, **fine).get_forces(torch.tensor(pos, device="cuda")).cpu().numpy()
+        atoms = rng.choice(len(num), size=8, replace=False)
+        for a in atoms:
+            for x in range(3):
+                an.append(f[a, x])
+                for sgn in (1.0, -1.0):
+                    p = pos.copy()
+                    p[a, x] += sgn * h
+                    geoms.append((num, p))
+    nb, pb = pad(geoms)
+    e = calc_for(nb, **fine).get_energy(torch.tensor(pb, device="cuda")).cpu().numpy()
     fd = -(e[0::2] - e[1::2]) / (2 * h)
-    an = np.array([f[a, x] for a in atoms for x in range(3)])
-    # the reference's energy carries ~1e-8 Eh noise from its Fermi tolerance
-    assert np.abs(fd - an).max() < 2e-4
-    assert np.median(np.abs(fd - an)) < 2e-5
+    err = np.abs(fd - np.array(an))
+    assert err.max() < 1e-6, err.max()
 
 
 def test_maxiter_warning_and_error():
@@ -249,12 +338,28 @@ def test_mixed_precision_same_fixed_point():
 def test_large_molecule_against_oracle():
     """A 300-atom molecule (~900 AOs): the block-wise Cholesky over the whole
     GPU, the global-memory lead-in of the on-chip FP32 tridiagonalisation
-    and the cluster FP64 passes, against the oracle."""
+    and the cluster FP64 passes, against the oracle.  If the engine's mixed
+    precision run ends in another SCF state than the oracle, the state must
+    be a genuine fixed point of the reference's equations, and the FP64-only
+    run (the oracle's own trajectory) must match the oracle."""
+    from tests.helpers import restart_energy
+    from tests.test_gpu_workloads import orbital_potential
+
     num, pos = molgen.grow(300, 4253)
-    calc = calc_for(num)
-    res = calc.singlepoint(torch.tensor(pos, device="cuda"), forces=True)
+    p = torch.tensor(pos, device="cuda")
     r = go.singlepoint(num, pos, mixer="broyden")
-    assert res.status[0] == 0 and r.converged
-    if same_state(res.energy.item(), r.energy):
-        assert abs(res.energy.item() - r.energy) < E_TOL
+    assert r.converged
+    res = calc_for(num).singlepoint(p, forces=True)
+    assert res.status[0] == 0
+    e = res.energy.item()
+    if same_state(e, r.energy):
+        assert abs(e - r.energy) < E_TOL
         assert np.abs(-res.gradient.cpu().numpy() - r.forces).max() < F_TOL
+    else:
+        assert abs(e - r.energy) > 1e-4
+        conv, it, er = restart_energy(num, pos, orbital_potential(num, res.shell_potential))
+        assert conv and it <= 40 and abs(er - e) < E_TOL
+    r64 = calc_for(num, mixed_precision=False).singlepoint(p, forces=True)
+    assert r64.status[0] == 0
+    assert abs(r64.energy.item() - r.energy) < E_TOL
+    assert np.abs(-r64.gradient.cpu().numpy() - r.forces).max() < F_TOL

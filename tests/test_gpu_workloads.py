@@ -1,22 +1,49 @@
 """Full-size workloads on the GPU against the reference's own results for
 every molecule (tests/golden/workload_*_ref.npz, produced by the reference).
 
-Molecules with several self-consistent solutions can end on different
-solutions in the reference (Anderson mixing) and in the engine (Broyden
-mixing).  For those the test checks that the engine's state is a genuine
-fixed point of the reference's equations: the oracle restarted from the
-engine's converged potential stays there and reproduces its energy."""
+Every molecule is classified and asserted:
+
+* both converged, same SCF state: |dE| <= 1e-8 Eh, atomic charges <= 1e-6 e,
+  and (force workload) forces within 1e-6 Eh/bohr of the reference's
+  analytical forces and of its autograd forces; where the autograd forces
+  differ by more (the reference's eigenvector derivative uses a Lorentzian
+  broadening that matters when the HOMO-LUMO gap is near kT), a five-point
+  finite difference of the energy decides, and the engine must be the
+  closer one and within 1e-6;
+* both converged, another SCF state (molecules with several self-consistent
+  solutions): the two energies must differ by more than 1e-4 Eh (a gap
+  between distinct solutions, not an imprecision), and the oracle restarted
+  from the engine's converged potential must stay there and reproduce the
+  engine's energy to 1e-8 Eh, i.e. the engine's state is a genuine fixed
+  point of the reference's equations;
+* converged by the reference only: not allowed;
+* converged by the engine only: the same fixed-point check;
+* converged by neither: nothing to compare (the reference returns its last
+  iterate, which depends on the trajectory).
+
+With ``mixer="anderson"`` and FP64 passes the engine replays the reference's
+own SCF trajectory (scf/mixer/anderson.py:200-317), so every molecule the
+reference converged must end in the same state.  With the engine's default
+(modified Broyden, FP32 early passes) some land on another solution, and
+those are checked as fixed points.
+"""
+import os
+import warnings
+
 import numpy as np
 import pytest
 import torch
 
 from dxtb_gb300 import molgen, params
-from oracle import gfn1_oracle as go
-from tests.helpers import GOLDEN, same_state
+from tests.helpers import GOLDEN, oracle_map, restart_energy, fd_force_component
 
 pytestmark = pytest.mark.gpu
 
 TIGHT = {"exclude": ["disp"], "maxiter": 300, "x_atol": 1e-10, "x_atol_max": 1e-10}
+MODES = {
+    "anderson_fp64": {"mixer": "anderson", "mixed_precision": False},
+    "broyden_mixed": {"mixer": "broyden", "mixed_precision": True},
+}
 
 
 def pad(mols):
@@ -43,20 +70,18 @@ def orbital_potential(numbers, vsh):
     return np.array(out)
 
 
-def run_workload(mols, forces):
+def run_workload(mols, forces, mode):
     from dxtb_gb300 import GFN1Calculator
 
     num, pos = pad(mols)
-    calc = GFN1Calculator(torch.as_tensor(num), opts=TIGHT)
-    import warnings
-
+    calc = GFN1Calculator(torch.as_tensor(num), opts={**TIGHT, **MODES[mode]})
     with warnings.catch_warnings():
         warnings.simplefilter("ignore")
         return calc.singlepoint(torch.tensor(pos, device="cuda"), forces=forces)
 
 
-def check_workload(mols, ref, forces, min_agree):
-    res = run_workload(mols, forces)
+def classify(mols, ref, forces, mode):
+    res = run_workload(mols, forces, mode)
     e = res.energy.cpu().numpy()
     q = res.charges.cpu().numpy()
     f = -res.gradient.cpu().numpy() if forces else None
@@ -64,77 +89,77 @@ def check_workload(mols, ref, forces, min_agree):
     assert np.array_equal(np.array([len(n) for n, _ in mols]), ref["natom"])
     aoff = np.concatenate([[0], np.cumsum(ref["natom"])])
     soff = np.concatenate([[0], np.cumsum([shells_of(n) for n, _ in mols])])
-    stats = {"same": 0, "other_state": 0, "ref_unconverged": 0, "engine_unconverged": 0}
-    restarts = 0
-    fd_checks = 0
-    worst = {"dE": 0.0, "dq": 0.0, "dF": 0.0}
+    stats = {"same": 0, "other_state": 0, "engine_only": 0, "neither": 0, "ref_only": [],
+             "iter_equal": 0, "autograd_outliers": 0}
+    worst = {"dE": 0.0, "dq": 0.0, "dF_analytical": 0.0, "dF_autograd": 0.0, "other_gap_min": np.inf}
+    restarts, fd_jobs = [], []
     for k, (num, pos) in enumerate(mols):
         a, b = aoff[k], aoff[k + 1]
-        if res.status[k] & 1:
-            stats["engine_unconverged"] += 1
+        assert res.status[k] & ~1 == 0, (k, res.status[k])
+        eng_conv = res.status[k] == 0
+        ref_conv = bool(ref["converged"][k])
+        if not eng_conv and not ref_conv:
+            stats["neither"] += 1
             continue
-        assert res.status[k] == 0
-        if not ref["converged"][k]:
-            stats["ref_unconverged"] += 1
+        if ref_conv and not eng_conv:
+            stats["ref_only"].append(k)
             continue
-        if same_state(e[k], ref["energy"][k]):
+        v = orbital_potential(num, vsh[soff[k]:soff[k + 1]])
+        if not ref_conv:
+            stats["engine_only"] += 1
+            restarts.append((k, num, pos, v, e[k]))
+            continue
+        de = abs(e[k] - ref["energy"][k])
+        if de < 1e-5:
             stats["same"] += 1
-            de = abs(e[k] - ref["energy"][k])
+            stats["iter_equal"] += int(res.iterations[k] == ref["iterations"][k])
             dq = np.abs(q[a:b] - ref["charges"][a:b]).max()
             worst["dE"] = max(worst["dE"], de)
             worst["dq"] = max(worst["dq"], dq)
-            assert de < 1e-8, k
-            assert dq < 1e-6, k
+            assert de <= 1e-8, (k, de)
+            assert dq <= 1e-6, (k, dq)
             if forces:
-                # the reference's analytical-gradient forces: same quantity
                 dfa = np.abs(f[a:b] - ref["forces_analytical"][a:b]).max()
-                worst["dF_analytical"] = max(worst.get("dF_analytical", 0.0), dfa)
-                assert dfa < 1e-6, k
-                # the reference's default autograd forces: equal up to the
-                # Lorentzian broadening of its eigenvector derivative, which
-                # matters when the HOMO-LUMO gap is near kT; central finite
-                # differences decide those cases
+                worst["dF_analytical"] = max(worst["dF_analytical"], dfa)
+                assert dfa <= 1e-6, (k, dfa)
                 dfg = np.abs(f[a:b] - ref["forces"][a:b])
-                worst["dF"] = max(worst["dF"], dfg.max())
-                if dfg.max() >= 1e-6:
-                    stats["autograd_outliers"] = stats.get("autograd_outliers", 0) + 1
-                    if fd_checks < 3:
-                        fd_checks += 1
-                        at, x = np.unravel_index(np.argmax(dfg), dfg.shape)
-                        # five-point central difference (truncation error O(h^4))
-                        # of the oracle energy with the electron count solved
-                        # to 1e-13: at the reference's sqrt(eps) Fermi
-                        # tolerance the energy carries ~5e-9 Eh of noise,
-                        # 5e-6 Eh/bohr after dividing by the step
-                        h = 5e-4
-                        efd = {}
-                        for st in (-2, -1, 1, 2):
-                            pp = pos.copy()
-                            pp[at, x] += st * h
-                            efd[st] = go.singlepoint(num, pp, mixer="broyden", forces=False,
-                                                     fermi_thr=1e-13).energy
-                        fd = -(8.0 * (efd[1] - efd[-1]) - (efd[2] - efd[-2])) / (12.0 * h)
-                        err_engine = abs(f[a + at, x] - fd)
-                        err_ref = abs(ref["forces"][a + at, x] - fd)
-                        assert err_engine < 1e-6 and err_engine < err_ref, (k, err_engine, err_ref)
+                worst["dF_autograd"] = max(worst["dF_autograd"], dfg.max())
+                if dfg.max() > 1e-6:
+                    stats["autograd_outliers"] += 1
+                    at, x = np.unravel_index(np.argmax(dfg), dfg.shape)
+                    fd_jobs.append((k, num, pos, int(at), int(x), f[a + at, x], ref["forces"][a + at, x]))
         else:
             stats["other_state"] += 1
-            if restarts < 2:
-                restarts += 1
-                v = orbital_potential(num, vsh[soff[k]:soff[k + 1]])
-                r = go.singlepoint(num, pos, mixer="broyden", v_init=v, forces=False, maxiter=30)
-                assert r.converged and r.iterations <= 40, k
-                assert abs(r.energy - e[k]) < 1e-8, k
-    print(stats, worst)
-    assert stats["same"] >= min_agree * len(mols)
+            worst["other_gap_min"] = min(worst["other_gap_min"], de)
+            assert de > 1e-4, (k, de)  # distinct solutions, not an imprecision
+            restarts.append((k, num, pos, v, e[k]))
+    # fixed-point checks of every engine state the reference did not reach
+    for (k, *_), (conv, it, er) in zip(restarts, oracle_map(restart_energy, [r[1:4] for r in restarts])):
+        assert conv and it <= 40, (k, conv, it)
+        assert abs(er - e[k]) <= 1e-8, (k, er, e[k])
+    # finite differences decide the autograd outliers
+    jobs = [(num, pos, at, x) for (_, num, pos, at, x, _, _) in fd_jobs]
+    for (k, _, _, at, x, fe, fr), fd in zip(fd_jobs, oracle_map(fd_force_component, jobs)):
+        err_engine, err_ref = abs(fe - fd), abs(fr - fd)
+        assert err_engine <= 1e-6 and err_engine < err_ref, (k, at, x, err_engine, err_ref)
+    print(mode, stats, worst)
+    # the engine converges every molecule the reference converges
+    assert stats["ref_only"] == [], stats["ref_only"]
     return stats
 
 
-def test_batch_workload_512():
+@pytest.mark.parametrize("mode", sorted(MODES))
+def test_batch_workload_512(mode):
     ref = np.load(GOLDEN / "workload_batch_ref.npz")
-    check_workload(molgen.c2_batch(512), ref, forces=False, min_agree=0.75)
+    stats = classify(molgen.c2_batch(512), ref, forces=False, mode=mode)
+    if mode == "anderson_fp64":
+        # replaying the reference's mixer, every molecule converged by both ends in the same state
+        assert stats["other_state"] == 0
 
 
-def test_forces_workload_256():
+@pytest.mark.parametrize("mode", sorted(MODES))
+def test_forces_workload_256(mode):
     ref = np.load(GOLDEN / "workload_forces_ref.npz")
-    check_workload(molgen.c3_forces(256), ref, forces=True, min_agree=0.85)
+    stats = classify(molgen.c3_forces(256), ref, forces=True, mode=mode)
+    if mode == "anderson_fp64":
+        assert stats["other_state"] == 0

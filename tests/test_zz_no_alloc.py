@@ -43,13 +43,12 @@ def make_plan(mols):
 
 
 def options(profile=0):
-    from dxtb_gb300 import _lib, params
+    from dxtb_gb300 import _lib
 
-    o = _lib.Options()
-    o.maxiter, o.fermi_maxiter, o.broyden_memory, o.want_forces = 300, 200, 20, 1
+    o = _lib.default_options()
+    o.maxiter, o.want_forces = 300, 1
     o.x_atol, o.x_atol_max = 1e-10, 1e-10
-    o.kt = 300.0 * params.KELVIN2AU
-    o.broyden_alpha = 0.3
+    o.mixer = _lib.MIXER_BROYDEN
     o.profile = profile
     o.mixed_precision = 1
     return o
@@ -82,11 +81,18 @@ def test_noalloc_matches_workspace_entry_point():
     _lib.check(lib.gbxtb_get_status(plan.handle, _lib.ptr(st, C.c_int32), None))
     assert (st == 0).all()
 
-    # two calls in a row without a workspace
-    for _ in range(2):
+    # two calls in a row without a workspace; the first one on this plan
+    # after the workspace call above instantiates the plan's pass graphs for
+    # the fixed scratch, the second must take no device memory at all
+    for call in range(2):
         e1, q1, g1 = outputs(plan)
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
         _lib.check(lib.gbxtb_singlepoint_noalloc(plan.handle, C.byref(opt), pos.data_ptr(), e1.data_ptr(),
                                                  q1.data_ptr(), g1.data_ptr(), stream))
+        torch.cuda.synchronize()
+        if call == 1:
+            assert torch.cuda.mem_get_info()[0] == free0
         st = np.zeros(plan.nmol, dtype=np.int32)
         _lib.check(lib.gbxtb_get_status(plan.handle, _lib.ptr(st, C.c_int32), None))
         assert (st == 0).all()
@@ -114,3 +120,22 @@ def test_noalloc_refuses_oversized_plans_and_profiling():
                                        q.data_ptr(), g.data_ptr(), stream)
     assert rc == -1  # GBXTB_ERR_ARG
     assert torch.isnan(e).all()  # nothing ran
+
+
+def test_noalloc_refuses_a_plan_of_another_device():
+    """The scratch is the current device's array: a plan made on another
+    device is refused before anything runs."""
+    if torch.cuda.device_count() < 2:
+        pytest.skip("needs two GPUs")
+    from dxtb_gb300 import _lib
+
+    lib = _lib.load()
+    with torch.cuda.device(1):
+        plan = make_plan(small_batch())
+    with torch.cuda.device(0):
+        e, q, g = outputs(plan)
+        pos = torch.zeros((plan.natom, 3), dtype=torch.float64, device="cuda:0")
+        rc = lib.gbxtb_singlepoint_noalloc(plan.handle, C.byref(options()), pos.data_ptr(), e.data_ptr(),
+                                           q.data_ptr(), g.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    assert rc == -1  # GBXTB_ERR_ARG
+    assert b"not the device of the plan" in lib.gbxtb_last_error()
