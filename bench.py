@@ -40,6 +40,15 @@ CPU_SAMPLE = 48           # molecules in the host-core baseline sample
 REF_STEP_SAMPLE = 24      # molecules per step of the reference arm
 PLAIN_SAMPLE = 24         # molecules timed one call each (the plain per-molecule GPU path)
 FP32_PER_FP64 = 64.0      # FP32 FMA per FP64 FMA of a GB300 SM (128 vs 2 per clock)
+# Speed of the numpy restatement against dxtb itself, measured once where
+# both run (x86 development host, one thread, the first 8 molecules of the
+# 512): the restatement took 9.1 s with forces, dxtb 14.5 s for energies
+# only (its recorded per-molecule seconds, tests/golden/workload_batch_ref.npz
+# cpu_seconds).  Timing the restatement therefore understates the speed-up
+# over the reference.
+PORT_VS_REFERENCE = ("numpy restatement 9.1 s (energy + forces) vs dxtb 14.5 s (energy only) on the first 8 "
+                     "molecules, one thread each, x86 development host: the restatement is ~1.6x faster "
+                     "than the reference itself")
 
 
 def workload_config(world: int, nmol: int = NMOL) -> dict:
@@ -182,6 +191,36 @@ def molecule_dims(mols):
     return n, np.ceil(nel / 2.0)
 
 
+def size_matched(mols, k: int) -> list[int]:
+    """Indices of k molecules at evenly spaced quantiles of the atom count,
+    so that a sample timed one by one has the size mix of the workload."""
+    order = np.argsort([len(m[0]) for m in mols], kind="stable")
+    return [int(order[i]) for i in np.linspace(0, len(mols) - 1, k).round().astype(int)]
+
+
+def parity_summary(res, ref, seconds: float) -> dict:
+    """Classification of every molecule against the reference's own results
+    (tests/golden/workload_batch_ref.npz): verified = both converged and
+    |dE| <= 1e-8 Eh; other_state = both converged on distinct SCF solutions
+    (|dE| > 1e-4 Eh; the GPU tests show each is a fixed point of the
+    reference's equations); imprecise = anything between, which must be 0."""
+    e = res.energy.cpu().numpy()
+    eng = res.status == 0
+    rc = ref["converged"]
+    both = eng & rc
+    d = np.abs(e - ref["energy"])
+    verified = both & (d <= 1e-8)
+    other = both & (d > 1e-4)
+    return {"molecules": int(len(e)), "engine_converged": int(eng.sum()), "reference_converged": int(rc.sum()),
+            "both_converged": int(both.sum()), "verified": int(verified.sum()),
+            "other_state": int(other.sum()), "imprecise": int((both & ~verified & ~other).sum()),
+            "reference_only_converged": int((rc & ~eng).sum()),
+            "max_dE_verified": float(d[verified].max()) if verified.any() else None,
+            "iterations_equal_to_reference": int((res.iterations[verified] == ref["iterations"][verified]).sum()),
+            "verified_rate": float(verified.sum() / seconds), "iterations_mean": float(res.iterations.mean()),
+            "iterations_max": int(res.iterations.max()), "fp32_passes_mean": float(res.fp32_passes.mean())}
+
+
 def pad(mols):
     nmax = max(len(m[0]) for m in mols)
     num = np.zeros((len(mols), nmax), dtype=np.int64)
@@ -219,7 +258,8 @@ def run_reference_arm(args, rank: int, world: int) -> None:
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port",
                          "sample": f"{REF_STEP_SAMPLE} molecules per step (consecutive slices of the 512), "
                                    "numpy restatement of the reference path incl. its Anderson mixer, "
-                                   "one process per core"},
+                                   "one process per core",
+                         "vs_reference_itself": PORT_VS_REFERENCE},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out), flush=True)
@@ -353,6 +393,8 @@ def main() -> None:
     ap.add_argument("--no-plain", action="store_true", help="skip the plain per-molecule GPU leg")
     ap.add_argument("--nmol", type=int, default=NMOL, help="molecules per GPU (profiling of smaller cases)")
     ap.add_argument("--fp64-only", action="store_true", help="disable the FP32 SCF passes")
+    ap.add_argument("--no-replay", action="store_true",
+                    help="skip the extra call with the reference's mixer (parity_reference_mixer)")
     ap.add_argument("--serve", action="store_true",
                     help="served stream instead of the batch: Poisson arrivals, 8-400 atoms, continuous batching")
     ap.add_argument("--serve-requests", type=int, default=96, help="requests per arrival rate")
@@ -391,7 +433,8 @@ def main() -> None:
         v, dt = cpu_throughput(mols[:CPU_SAMPLE], procs)
         cpu = {"value": v, "unit": UNIT, "cores": procs, "kind": "port",
                "sample": f"first {CPU_SAMPLE} of the 512 molecules, energy + forces, numpy restatement of "
-                         f"the reference path incl. its Anderson mixer, one process per core ({dt:.1f} s)"}
+                         f"the reference path incl. its Anderson mixer, one process per core ({dt:.1f} s)",
+               "vs_reference_itself": PORT_VS_REFERENCE}
 
     import torch
     import torch.distributed as dist
@@ -464,10 +507,11 @@ def main() -> None:
     nbytes_out = e_host.numel() * 8 + f_host.numel() * 8
     e2e = replicas.whole_job_rate(nmol, world, args.steps, t_e2e)
 
-    # the plain per-molecule GPU path: one engine call per molecule
+    # the plain per-molecule GPU path: one engine call per molecule, on a
+    # size-matched sample (evenly spaced quantiles of the atom count)
     plain = None
     if not args.no_plain:
-        sample = mols[:PLAIN_SAMPLE]
+        sample = [mols[i] for i in size_matched(mols, PLAIN_SAMPLE)]
         calcs = [GFN1Calculator(torch.as_tensor(a), opts=run_opts) for a, _ in sample]
         poss = [torch.tensor(b, device=dev) for _, b in sample]
         for c, p in zip(calcs, poss):  # warm (plans, workspaces)
@@ -480,27 +524,32 @@ def main() -> None:
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
         plain = {"value": len(sample) / dt, "unit": UNIT,
-                 "sample": f"first {len(sample)} molecules of the workload, one engine call each "
-                           "(device-resident positions, gradient read back per call)",
+                 "sample": f"{len(sample)} molecules of the workload at evenly spaced quantiles of the "
+                           "atom count, one engine call each (device-resident positions, gradient read "
+                           "back per call)",
                  "batched_over_plain": value / (len(sample) / dt)}
 
-    # parity summary of this run against the reference's own results (rank 0 set)
-    parity = None
+    # parity of this run against the reference's own results (rank 0 set),
+    # and of one call that replays the reference's own SCF (its Anderson
+    # mixer, every pass in FP64), outside the timed region
+    parity = replay = None
     ref_path = ROOT / "tests" / "golden" / "workload_batch_ref.npz"
     if rank == 0 and ref_path.exists() and nmol == NMOL:
         ref = np.load(ref_path)
-        e = res.energy.cpu().numpy()
-        ok = (res.status == 0) & ref["converged"]
-        d = np.abs(e - ref["energy"])
-        same = ok & (d < 1e-5)
-        parity = {"molecules": NMOL, "engine_converged": int((res.status == 0).sum()),
-                  "reference_converged": int(ref["converged"].sum()),
-                  "same_scf_state": int(same.sum()),
-                  "within_1e-8": int((same & (d <= 1e-8)).sum()),
-                  "max_dE_same_state": float(d[same].max()) if same.any() else None,
-                  "iterations_mean": float(res.iterations.mean()),
-                  "iterations_max": int(res.iterations.max()),
-                  "fp32_passes_mean": float(res.fp32_passes.mean())}
+        parity = parity_summary(res, ref, t_dev / args.steps)
+        if not args.no_replay:
+            calc_r = GFN1Calculator(torch.as_tensor(num), opts={**OPTS, "mixer": "anderson",
+                                                                 "mixed_precision": False})
+            calc_r.singlepoint(pos_dev, forces=True)
+            er0 = torch.cuda.Event(enable_timing=True)
+            er1 = torch.cuda.Event(enable_timing=True)
+            er0.record()
+            rr = calc_r.singlepoint(pos_dev, forces=True)
+            er1.record()
+            torch.cuda.synchronize()
+            t_r = er0.elapsed_time(er1) / 1e3
+            replay = {"mode": "mixer=anderson (the reference's), every SCF pass in FP64", "seconds": t_r,
+                      "rate": NMOL / t_r, **parity_summary(rr, ref, t_r)}
 
     # roofline of the dominant kernel class: FP64-pipe-equivalent rate
     # (an FP32 FMA counts 1/64 of an FP64 FMA, the ratio of the two pipes)
@@ -538,6 +587,7 @@ def main() -> None:
             "roofline": roof,
             "stage_ms_per_step": {k: round(v, 3) for k, v in per_step_ms.items()},
             "parity": parity,
+            "parity_reference_mixer": replay,
             "plain_per_molecule": plain,
             "mixed_precision": not args.fp64_only,
             "autotuned": {"tridiag_warps_per_size_class": next(iter(calc._plans.values())).tuned[:3],

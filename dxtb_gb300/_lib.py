@@ -18,6 +18,7 @@ MOL_NOT_CONVERGED = 1
 MOL_FERMI_FAIL = 2
 MOL_CHOLESKY_FAIL = 4
 MOL_NONFINITE = 8
+MOL_RESTARTED = 16
 
 EXPORTED = (
     "gbxtb_version", "gbxtb_last_error", "gbxtb_ctx_create", "gbxtb_ctx_destroy",
@@ -70,9 +71,11 @@ class Options(C.Structure):
         ("soft_start", C.c_int32),
         ("mix_guess", C.c_int32),
         ("damp_dynamic", C.c_int32),
-        ("reserved", C.c_int32),
+        ("no_halogen", C.c_int32),
         ("damp_dynamic_factor", C.c_double),
         ("fermi_thresh", C.c_double),
+        ("restart_at", C.c_int32),
+        ("reserved", C.c_int32),
     ]
 
 

@@ -59,6 +59,10 @@ DEFAULT_OPTS = {
     "mixer": "broyden",
     "broyden_alpha": 0.3,
     "broyden_memory": 20,
+    # Broyden/simple: a molecule still iterating after this many passes is
+    # solved again from the guess with the reference's Anderson mixer (FP64),
+    # so that it follows the reference's own SCF; 0: never
+    "anderson_restart": 0,
     "damp": 0.5,                    # DAMP
     "damp_init": 0.1,               # DAMP_INIT
     "damp_generations": 5,          # DAMP_GENERATIONS
@@ -220,7 +224,7 @@ def _register_fakes() -> None:
 def _pack_options(o: _lib.Options) -> tuple[list[int], list[float]]:
     """The option vectors of ``gbxtb::singlepoint`` (order in torch_ops.cpp)."""
     iopts = [o.maxiter, o.fermi_maxiter, o.broyden_memory, o.want_forces, o.profile, o.mixed_precision,
-             o.mixer, o.generations, o.soft_start, o.mix_guess, o.damp_dynamic]
+             o.mixer, o.generations, o.soft_start, o.mix_guess, o.damp_dynamic, o.no_halogen, o.restart_at]
     fopts = [o.x_atol, o.x_atol_max, o.kt, o.broyden_alpha, o.damp, o.damp_init, o.diagonal_offset,
              o.damp_dynamic_factor, o.fermi_thresh]
     return [int(x) for x in iopts], [float(x) for x in fopts]
@@ -266,8 +270,11 @@ def resolve_opts(opts: dict | None) -> dict:
             "D3 dispersion is not available in this engine (its reference data is not "
             "distributed with the model); pass opts={'exclude': ['disp']}"
         )
-    if {"es2", "es3", "rep", "scf", "all", "hcore"} & excl:
-        raise NotImplementedError(f"excluding {sorted(excl - {'disp', 'halogen'})} is not supported")
+    # "hal" switches the halogen-bond term off; "aes2" and "d4sc" name GFN2
+    # terms that GFN1 does not have (types/base.py:594-651)
+    unsupported = excl - {"disp", "hal", "aes2", "d4sc"}
+    if unsupported:
+        raise NotImplementedError(f"excluding {sorted(unsupported)} is not supported")
     o["exclude"] = sorted(excl)
     if o["guess"] == "eeq":
         raise ValueError(
@@ -279,6 +286,8 @@ def resolve_opts(opts: dict | None) -> dict:
         raise ValueError("damp_generations must be in 1..28")
     if not 1 <= int(o["broyden_memory"]) <= 29:
         raise ValueError("broyden_memory must be in 1..29")
+    if int(o["anderson_restart"]) < 0:
+        raise ValueError("anderson_restart must be >= 0")
     return o
 
 
@@ -306,6 +315,8 @@ def engine_options(o: dict, forces: bool) -> _lib.Options:
     opt.damp_dynamic = 1 if o["damp_dynamic"] else 0
     opt.damp_dynamic_factor = float(o["damp_dynamic_factor"])
     opt.fermi_thresh = 0.0 if o["fermi_thresh"] is None else float(o["fermi_thresh"])
+    opt.no_halogen = 1 if "hal" in o["exclude"] else 0
+    opt.restart_at = int(o["anderson_restart"])
     return opt
 
 

@@ -115,6 +115,10 @@ int check_options(const gbxtb_options *o) {
       return fail(GBXTB_ERR_ARG, "unknown mixer " + std::to_string(o->mixer));
   }
   if (!std::isfinite(o->fermi_thresh)) return fail(GBXTB_ERR_ARG, "fermi_thresh must be finite");
+  if (o->restart_at < 0) return fail(GBXTB_ERR_ARG, "restart_at must be >= 0");
+  if (o->restart_at > 0 && (o->generations < 1 || o->generations > kHistMax - 1 || !std::isfinite(o->damp) ||
+                            !std::isfinite(o->damp_init) || !std::isfinite(o->diagonal_offset)))
+    return fail(GBXTB_ERR_ARG, "restart_at needs valid Anderson options (generations, damp, damp_init, offset)");
   if (o->damp_dynamic && !std::isfinite(o->damp_dynamic_factor))
     return fail(GBXTB_ERR_ARG, "damp_dynamic_factor must be finite");
   return GBXTB_OK;
@@ -473,7 +477,7 @@ namespace {
 int enqueue_setup(gbxtb_plan *plan, const Work &w, const gbxtb_options &o, const double *positions_dev,
                   cudaStream_t s, Prof &pf) {
   const DevPlan &pl = plan->pl;
-  const DevParams &p = plan->ctx->p;
+  const DevParams p = call_params(plan->ctx->p, o);
   const gbxtb_options *opts = &o;
   // reset state
   CK(cudaMemsetAsync(w.status, 0, sizeof(int32_t) * pl.nmol, s));
@@ -485,6 +489,7 @@ int enqueue_setup(gbxtb_plan *plan, const Work &w, const gbxtb_options &o, const
   CK(cudaMemsetAsync(w.stall32, 0, sizeof(int32_t) * pl.nmol, s));
   CK(cudaMemsetAsync(w.mixstep, 0, sizeof(int32_t) * pl.nmol, s));
   CK(cudaMemsetAsync(w.dampsw, 0, sizeof(int32_t) * pl.nmol, s));
+  CK(cudaMemsetAsync(w.mixsel, 0, sizeof(int32_t) * pl.nmol, s));
   CK(cudaMemsetAsync(w.best32, 0x7f, sizeof(double) * pl.nmol, s));  // 1.4e306: no pass yet
   // 0: the first passes run in FP32; any non-zero byte pattern means FP64
   CK(cudaMemsetAsync(w.prec, opts->mixed_precision ? 0 : 1, sizeof(int32_t) * pl.nmol, s));
@@ -581,7 +586,7 @@ int gbxtb_singlepoint(gbxtb_plan *plan, const gbxtb_options *opts, const double 
   if (rc) return rc;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const DevPlan &pl = plan->pl;
-  const DevParams &p = plan->ctx->p;
+  const DevParams p = call_params(plan->ctx->p, *opts);
   if (opts->profile && !plan->ev_ready) {
     for (int c = 0; c < GBXTB_PROF_CLASSES; ++c)
       for (int k = 0; k < 2; ++k) CK(cudaEventCreate(&plan->ev[c][k]));
@@ -681,6 +686,7 @@ int gbxtb_singlepoint(gbxtb_plan *plan, const gbxtb_options *opts, const double 
   plan->last_stream = s;
   plan->last_work = w;
   plan->last_ws = workspace_dev;
+  plan->last_opts = *opts;
   plan->has_run = true;
   return GBXTB_OK;
 }
@@ -696,7 +702,7 @@ int gbxtb_forces(gbxtb_plan *plan, const double *positions_dev, double *gradient
   if (rc) return rc;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   launch_gemm(plan->pl, w, plan->tile0, plan->ntile, 4, 1, s);
-  launch_forces(plan->ctx->p, plan->pl, w, positions_dev, gradient_dev, s);
+  launch_forces(call_params(plan->ctx->p, plan->last_opts), plan->pl, w, positions_dev, gradient_dev, s);
   CK(cudaGetLastError());
   plan->last_stream = s;
   return GBXTB_OK;

@@ -80,6 +80,7 @@ struct gbxtb_plan {
   cudaStream_t last_stream = nullptr;
   gbxtb::Work last_work{};
   void *last_ws = nullptr;  // workspace of the last singlepoint (its final SCF state)
+  gbxtb_options last_opts{};  // options of the last singlepoint
   bool has_run = false;
   int32_t *h_active = nullptr;  // pinned
   int num_sms = 0;
@@ -127,7 +128,7 @@ inline Layout make_layout(const DevPlan &pl) {
   L.add(d * pl.ngam);                                       // gam
   for (int k = 0; k < 4; ++k) L.add(d * pl.natom);          // cn erep qat dedcn
   L.add(d * 3 * pl.natom);                                  // grad
-  for (int k = 0; k < 10; ++k) L.add(i4 * pl.nmol);  // status phase iter kvec nhist prec npass32 stall32 mixstep dampsw
+  for (int k = 0; k < 11; ++k) L.add(i4 * pl.nmol);  // status phase iter kvec nhist prec npass32 stall32 mixstep dampsw mixsel
   L.add(d * 2 * pl.nmol);                                   // efermi
   L.add(d * 6 * pl.nmol);                                   // energy
   L.add(d * 2 * pl.nmol);                                   // resid
@@ -159,6 +160,7 @@ inline Work make_work(const DevPlan &pl, void *base) {
   w.stall32 = I();
   w.mixstep = I();
   w.dampsw = I();
+  w.mixsel = I();
   w.efermi = D(); w.energy = D(); w.resid = D(); w.best32 = D();
   w.active = I();
   w.active_list = I();

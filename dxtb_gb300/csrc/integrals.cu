@@ -5,6 +5,9 @@
 // Reference behaviour reproduced (dxtb, src/dxtb/_src/...):
 //   CN            xtb/gfn1.py:62-64 (D3 counting, exponential, 25 bohr cutoff)
 //   repulsion     components/classicals/repulsion/base.py:173-406, rep.py:60-95
+//   halogen bond  components/classicals/halogen/hal.py:168-364 (donors Cl, Br,
+//                 I, At; acceptors N, O, P, S within 20 bohr; the donor's
+//                 nearest atom sets the angle), with its analytic gradient
 //   overlap       integral/driver/pytorch/impls/overlap.py:147-243 (pairs with
 //                 0.1 < R < 50 bohr; same-atom blocks are the identity),
 //                 impls/md/explicit.py:61-187, impls/md/trafo.py:63-182
@@ -42,12 +45,18 @@ __device__ __forceinline__ void cart_exp(int l, int c, int &ex, int &ey, int &ez
 }
 
 // Cartesian -> real spherical for one index: p ordered (y, z, x); d ordered
-// (z2, xz, yz, x2-y2, xy) with the normalisation of trafo.py:63-90.
+// (z2, xz, yz, x2-y2, xy) with the normalisation of trafo.py:63-90.  The
+// reference keeps its double factorials (basis/slater.py:53-55) and that
+// table in float32: its d shells are normalised with 1/float32(sqrt(3)) and
+// the xy-type rows carry float32(sqrt(3)), which cancel, but its d_z2
+// function keeps a factor sqrt(3)/float32(sqrt(3)) = 1 + 1.8e-8 (kDz2).  It
+// is reproduced, since every d-shell integral and energy carries it.
 __device__ __forceinline__ void to_sph(int l, const double *c, double *s) {
   if (l == 0) { s[0] = c[0]; return; }
   if (l == 1) { s[0] = c[1]; s[1] = c[2]; s[2] = c[0]; return; }
   const double s3 = 1.7320508075688772, s3h = 0.8660254037844386;
-  s[0] = -0.5 * c[0] - 0.5 * c[1] + c[2];
+  const double kDz2 = 1.0000000179482318;  // sqrt(3) / float32(sqrt(3))
+  s[0] = (-0.5 * c[0] - 0.5 * c[1] + c[2]) * kDz2;
   s[1] = s3 * c[4];
   s[2] = s3 * c[5];
   s[3] = s3h * (c[0] - c[1]);
@@ -196,7 +205,78 @@ __device__ __forceinline__ void decode_pair(int64_t k, int n, int &i, int &j) {
 }
 
 // ---------------------------------------------------------------------------
-// per-atom kernel: coordination number and repulsion energy
+// halogen bond (hal.py:168-364).  For a donor X (Cl, Br, I, At) with bond
+// strength xb, every acceptor J (N, O, P, S) within the cutoff and the atom K
+// nearest to X (the first of equals, at a non-zero distance) contribute
+//   E_X += xb lj(R_XJ) ((1 - c) / 2)^6,   c = cos(angle J-X-K),
+//   lj(R) = (s^12 - damp s^6) / (1 + s^12),  s = rscale (R_X + R_J) / R
+// (the reference writes (1 - c) / 2 as 0.5 - 0.25 cosa, cosa = 2c by the
+// rule of cosines).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool xb_donor(int z) { return z == 17 || z == 35 || z == 53 || z == 85; }
+__device__ __forceinline__ bool xb_acceptor(int z) { return z == 7 || z == 8 || z == 15 || z == 16; }
+
+// Nearest atom to donor a of molecule md (hal.py:241-250); the molecule's
+// first atom if none lies at a non-zero distance.
+__device__ int xb_nearest(const MolDesc &md, const double *__restrict__ pos, int a) {
+  int best = md.atom0;
+  double dist = 1.79769313486231570e308;
+  for (int ib = 0; ib < md.natom; ++ib) {
+    const int b = md.atom0 + ib;
+    const double dx = pos[3 * b] - pos[3 * a], dy = pos[3 * b + 1] - pos[3 * a + 1],
+                 dz = pos[3 * b + 2] - pos[3 * a + 2];
+    const double r = sqrt(dx * dx + dy * dy + dz * dz);
+    if (0.0 < r && r < dist) {
+      best = b;
+      dist = r;
+    }
+  }
+  return best;
+}
+
+// One donor-acceptor term; with grad, dE/dX, dE/dJ, dE/dK are accumulated
+// into gx[3], gj[3], gk[3].
+template <bool kGrad>
+__device__ double xb_term(const DevParams &p, const double *__restrict__ pos, int x, int j, int k, int zx,
+                          int zj, double *gx, double *gj, double *gk) {
+  const double *ex = p.elem_data + (size_t)zx * GBXTB_ELEM_DOUBLES;
+  const double *ej = p.elem_data + (size_t)zj * GBXTB_ELEM_DOUBLES;
+  const double damp = p.g[12], rscale = p.g[13];
+  const double r0 = rscale * (ex[5] + ej[5]);
+  double u[3], v[3];
+  for (int c = 0; c < 3; ++c) {
+    u[c] = pos[3 * j + c] - pos[3 * x + c];
+    v[c] = pos[3 * k + c] - pos[3 * x + c];
+  }
+  const double uu = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+  const double vv = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+  const double uv = u[0] * v[0] + u[1] * v[1] + u[2] * v[2];
+  const double ru = sqrt(uu), rv = sqrt(vv);
+  const double s = r0 / ru, s6 = s * s * s * s * s * s, s12 = s6 * s6;
+  const double lj = (s12 - damp * s6) / (1.0 + s12);
+  const double cs = uv / sqrt(uu * vv);
+  const double h = 0.5 - 0.5 * cs, h2 = h * h, h5 = h2 * h2 * h;
+  const double fd = h5 * h;
+  const double xb = ex[7];
+  if (kGrad) {
+    // d lj / d R and d fd / d c
+    const double dlj = -(12.0 * s12 - 6.0 * damp * s6 + 6.0 * damp * s6 * s12) / (ru * (1.0 + s12) * (1.0 + s12));
+    const double dfd = -3.0 * h5;
+    for (int c = 0; c < 3; ++c) {
+      const double dcdu = v[c] / (ru * rv) - cs * u[c] / uu;
+      const double dcdv = u[c] / (ru * rv) - cs * v[c] / vv;
+      const double du = xb * (dlj * u[c] / ru * fd + lj * dfd * dcdu);
+      const double dv = xb * lj * dfd * dcdv;
+      gj[c] += du;
+      gk[c] += dv;
+      gx[c] -= du + dv;
+    }
+  }
+  return xb * lj * fd;
+}
+
+// ---------------------------------------------------------------------------
+// per-atom kernel: coordination number, repulsion and halogen-bond energy
 // ---------------------------------------------------------------------------
 __global__ void k_atoms(DevParams p, DevPlan pl, Work w, const double *__restrict__ pos) {
   const int m = blockIdx.x;
@@ -236,8 +316,21 @@ __global__ void k_atoms(DevParams p, DevPlan pl, Work w, const double *__restric
         erep += ea[2] * eb[2] * exp(-alpha * pow(r, kexp)) / r;
       }
     }
+    // halogen bond, attributed to the donor (hal.py:359)
+    double exb = 0.0;
+    if (p.g[15] == 0.0 && xb_donor(za) && ea[7] != 0.0) {
+      const int k = xb_nearest(md, pos, a);
+      for (int ib = 0; ib < md.natom; ++ib) {
+        const int b = md.atom0 + ib;
+        const int zb = pl.atom_z[b];
+        if (!xb_acceptor(zb)) continue;
+        const double dx = pos[3 * b] - xa, dy = pos[3 * b + 1] - ya, dz = pos[3 * b + 2] - za_;
+        if (sqrt(dx * dx + dy * dy + dz * dz) > p.g[14]) continue;
+        exb += xb_term<false>(p, pos, a, b, k, za, zb, nullptr, nullptr, nullptr);
+      }
+    }
     w.cn[a] = cn;
-    w.erep[a] = 0.5 * erep;
+    w.erep[a] = 0.5 * erep + exb;  // classical energy of the atom
   }
 }
 
@@ -446,6 +539,28 @@ __global__ void k_force_atoms(DevParams p, DevPlan pl, Work w, const double *__r
       t -= v.kcn * w.dedh[sh];
     }
     w.dedcn[a] = t;
+    // halogen bond: the donor's terms move the donor, the acceptor and the
+    // donor's nearest atom
+    const int za = pl.atom_z[a];
+    if (p.g[15] == 0.0 && xb_donor(za) && p.elem_data[(size_t)za * GBXTB_ELEM_DOUBLES + 7] != 0.0) {
+      const int k = xb_nearest(md, pos, a);
+      double gx[3] = {0.0, 0.0, 0.0};
+      for (int ib = 0; ib < md.natom; ++ib) {
+        const int b = md.atom0 + ib;
+        const int zb = pl.atom_z[b];
+        if (!xb_acceptor(zb)) continue;
+        const double dx = pos[3 * b] - pos[3 * a], dy = pos[3 * b + 1] - pos[3 * a + 1],
+                     dz = pos[3 * b + 2] - pos[3 * a + 2];
+        if (sqrt(dx * dx + dy * dy + dz * dz) > p.g[14]) continue;
+        double gj[3] = {0.0, 0.0, 0.0}, gk[3] = {0.0, 0.0, 0.0};
+        xb_term<true>(p, pos, a, b, k, za, zb, gx, gj, gk);
+        for (int c = 0; c < 3; ++c) {
+          atomicAdd(&w.grad[3 * b + c], gj[c]);
+          atomicAdd(&w.grad[3 * k + c], gk[c]);
+        }
+      }
+      for (int c = 0; c < 3; ++c) atomicAdd(&w.grad[3 * a + c], gx[c]);
+    }
   }
   __syncthreads();
   for (int ia = threadIdx.x; ia < md.natom; ia += blockDim.x) {

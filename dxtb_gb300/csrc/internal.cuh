@@ -117,6 +117,7 @@ struct Work {
   int32_t *status, *phase, *iter, *kvec, *nhist;
   int32_t *mixstep; // mixer calls made (the reference mixer's iter_step)
   int32_t *dampsw;  // 1: damp_dynamic has switched the mixing parameter
+  int32_t *mixsel;  // 1: restarted with the reference's Anderson mixer (restart_at)
   int32_t *prec;    // 0: the next pass runs in FP32, 1: in FP64
   int32_t *npass32; // number of FP32 passes the molecule made
   int32_t *stall32; // FP32 passes since the potential change last halved
@@ -236,6 +237,14 @@ constexpr int kFailBits = GBXTB_MOL_FERMI_FAIL | GBXTB_MOL_CHOLESKY_FAIL | GBXTB
 // in a pool only on the molecules that converged in this step.
 __device__ __forceinline__ bool force_due(const DevPlan &pl, const Work &w, int m) {
   return pl.pool ? w.phase[m] == kPhaseFinished : (w.status[m] & kFailBits) == 0;
+}
+
+// Parameters of one call: the context's tables with the call's switches in
+// the spare global slot (g[15] = 1: no halogen-bond term).
+inline DevParams call_params(const DevParams &p, const gbxtb_options &o) {
+  DevParams c = p;
+  c.g[15] = o.no_halogen ? 1.0 : 0.0;
+  return c;
 }
 
 // ---------------------------------------------------------------------------

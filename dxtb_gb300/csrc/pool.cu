@@ -51,6 +51,7 @@ __global__ void k_pool_reset(DevPlan pl, Work w, const int32_t *slots, int n, in
     w.stall32[m] = 0;
     w.mixstep[m] = 0;
     w.dampsw[m] = 0;
+    w.mixsel[m] = 0;
     w.best32[m] = 1.0e300;
     for (int c = 0; c < 6; ++c) w.energy[(size_t)m * 6 + c] = 0.0;
   }
@@ -396,7 +397,7 @@ int gbxtb_pool_step_launch(gbxtb_pool *pool, void *stream) {
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   gbxtb_plan *plan = pool->plan;
   const DevPlan &pl = plan->pl;
-  const DevParams &p = plan->ctx->p;
+  const DevParams p = call_params(plan->ctx->p, pool->opts);
   const Work &w = pool->w;
   const gbxtb_options &o = pool->opts;
   const int nadm = (int)pool->pending.size();

@@ -127,7 +127,7 @@ struct MixOpts {
   double x_atol, x_atol_max, alpha, w0, kt;
   double damp, damp_init, offset, damp_dyn;
   int maxiter, memory;
-  int mixer, generations, soft_start, mix_guess, damp_dynamic;
+  int mixer, generations, soft_start, mix_guess, damp_dynamic, restart_at;
 };
 
 constexpr int kMixThreads = 256;
@@ -474,6 +474,20 @@ __global__ void __launch_bounds__(kMixThreads) k_charges_mix(DevParams p, DevPla
       w.prec[m] = 1;
       w.npass32[m] = iter + 1;
     }
+    // restart_at: still iterating after that many passes with a mixer other
+    // than Anderson, the molecule starts again from the guess with the
+    // reference's Anderson mixer, every pass in FP64
+    if (flag == 0 && o.restart_at > 0 && !w.mixsel[m] && o.mixer != GBXTB_MIXER_ANDERSON &&
+        iter + 1 >= o.restart_at) {
+      if (lowp) w.npass32[m] = iter + 1;
+      flag = 4;
+      w.mixsel[m] = 1;
+      w.prec[m] = 1;
+      w.mixstep[m] = 0;
+      w.nhist[m] = 0;
+      w.dampsw[m] = 0;
+      w.status[m] |= GBXTB_MOL_RESTARTED;
+    }
     s_flag = flag;
     if (flag == 3) {
       w.status[m] |= GBXTB_MOL_NONFINITE;
@@ -482,11 +496,15 @@ __global__ void __launch_bounds__(kMixThreads) k_charges_mix(DevParams p, DevPla
       if (flag == 2) w.status[m] |= GBXTB_MOL_NOT_CONVERGED;
       w.phase[m] = kPhaseFinal;
     }
-    w.iter[m] = iter + 1;
+    w.iter[m] = (flag == 4) ? 0 : iter + 1;
   }
   __syncthreads();
   const int flag = s_flag;
   if (flag == 3) return;
+  if (flag == 4) {
+    for (int i = threadIdx.x; i < nsh; i += blockDim.x) vin[i] = 0.0;  // the guess (SAD)
+    return;
+  }
   if (flag) {
     for (int i = threadIdx.x; i < nsh; i += blockDim.x) vin[i] = vout[i];
     return;
@@ -501,9 +519,10 @@ __global__ void __launch_bounds__(kMixThreads) k_charges_mix(DevParams p, DevPla
   }
   const int step = w.mixstep[m];  // mixer calls before this one
   const double damp = w.dampsw[m] ? o.damp_dyn : o.damp;
-  if (o.mixer == GBXTB_MIXER_ANDERSON) {
+  const int mixer = w.mixsel[m] ? GBXTB_MIXER_ANDERSON : o.mixer;
+  if (mixer == GBXTB_MIXER_ANDERSON) {
     anderson_step(pl, w, md, o, step, damp, a);
-  } else if (o.mixer == GBXTB_MIXER_SIMPLE) {
+  } else if (mixer == GBXTB_MIXER_SIMPLE) {
     for (int i = threadIdx.x; i < nsh; i += blockDim.x) vin[i] = vin[i] + (vout[i] - vin[i]) * damp;
   } else {
     broyden_step(pl, w, md, m, o, step, a);
@@ -591,6 +610,7 @@ void launch_charges_mix(const DevParams &p, const DevPlan &pl, const Work &w,
   mo.soft_start = o.soft_start;
   mo.mix_guess = o.mix_guess;
   mo.damp_dynamic = o.damp_dynamic;
+  mo.restart_at = o.restart_at;
   k_charges_mix<<<pl.nmol, kMixThreads, 0, s>>>(p, pl, w, mo);
 }
 

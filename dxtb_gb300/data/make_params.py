@@ -51,6 +51,8 @@ def main(src: str) -> None:
         "gexp": toml["charge"]["effective"]["gexp"],
         "average": toml["charge"]["effective"]["average"],
         "thirdorder_shell": toml["thirdorder"]["shell"],
+        "halogen": {"damping": toml["halogen"]["classical"]["damping"],
+                    "rscale": toml["halogen"]["classical"]["rscale"]},
         "kpair": {},
         "elements": {},
         "sto": {},
@@ -81,7 +83,7 @@ def main(src: str) -> None:
             seen.add(l)
         out["elements"][str(z)] = {
             "symbol": sym, "shells": shells, "gam": el["gam"], "gam3": el["gam3"],
-            "zeff": el["zeff"], "arep": el["arep"], "en": el["en"],
+            "zeff": el["zeff"], "arep": el["arep"], "en": el["en"], "xbond": el.get("xbond", 0.0),
         }
     OUT.write_text(json.dumps(out, indent=1, sort_keys=True))
     print(f"wrote {OUT} ({OUT.stat().st_size} bytes)")

@@ -101,3 +101,34 @@ def c4_stream(count: int) -> list:
 def c5_large(count: int = 16) -> list:
     """Molecules of 1000-2000 atoms."""
     return workload(4, count, 1000, 2000)
+
+
+# Halogen donors for the halogen-bond molecules and their bond length to a
+# heavy atom (bohr).
+HALOGEN_BOND = {35: 3.65, 53: 4.05}
+
+
+def halogenated(natoms: int, seed: int, nhal: int = 2) -> tuple[np.ndarray, np.ndarray]:
+    """A grown CHNO molecule in which ``nhal`` hydrogens become Br or I
+    (chosen with equal probability), moved out along their bond to the
+    halogen's bond length; a hydrogen whose halogen would come within 2.2
+    bohr of another atom is left in place.  Br and I have odd valence
+    counts like H, so the molecule stays a closed shell."""
+    num, pos = grow(natoms, seed)
+    num, pos = num.copy(), pos.copy()
+    rng = np.random.Generator(np.random.PCG64(seed + 777_000))
+    heavy = np.flatnonzero(num != 1)
+    done = 0
+    for h in rng.permutation(np.flatnonzero(num == 1)):
+        if done == nhal:
+            break
+        z = int(rng.choice(list(HALOGEN_BOND)))
+        anchor = heavy[np.argmin(np.linalg.norm(pos[heavy] - pos[h], axis=1))]
+        d = pos[h] - pos[anchor]
+        cand = pos[anchor] + HALOGEN_BOND[z] * d / np.linalg.norm(d)
+        others = np.delete(np.arange(len(num)), [h, anchor])
+        if np.min(np.linalg.norm(pos[others] - cand, axis=1)) < MIN_DIST:
+            continue
+        num[h], pos[h] = z, cand
+        done += 1
+    return num, pos

@@ -49,6 +49,10 @@ CN_STEEPNESS = 16.0
 CN_CUTOFF = 25.0
 REPULSION_CUTOFF = 25.0
 INTEGRAL_CUTOFF = 50.0
+XB_CUTOFF = 20.0  # halogen-bond pair cutoff in bohr (constants/xtb.py:33)
+# halogen-bond donors and acceptors (components/classicals/halogen/hal.py:117-118)
+XB_DONORS = (17, 35, 53, 85)
+XB_ACCEPTORS = (7, 8, 15, 16)
 
 ATOMIC_RADII_AA = (
     0.32, 0.37, 1.30, 0.99, 0.84, 0.75, 0.71, 0.64, 0.60, 0.62,
@@ -140,7 +144,8 @@ def tables() -> Tables:
         if el is None:
             continue
         elem_data[z] = [el["gam"], el["gam3"], el["zeff"], el["arep"], el["en"],
-                        ATOMIC_RADII_AA[z - 1] * AA2AU, COV_D3_AA[z - 1] * (4.0 / 3.0) * AA2AU, 0.0]
+                        ATOMIC_RADII_AA[z - 1] * AA2AU, COV_D3_AA[z - 1] * (4.0 / 3.0) * AA2AU,
+                        el.get("xbond", 0.0)]
         elem_shell0[z] = len(shell_int)
         shells = contracted_shells(z)
         elem_nshell[z] = len(shells)
@@ -164,8 +169,9 @@ def tables() -> Tables:
         kpair[a, b] = kpair[b, a] = val
     sh = par["shell"]
     g = np.zeros(GLOBALS)
-    g[:12] = [par["kpol"], par["enscale"], sh["ss"], sh["pp"], sh["dd"], sh["sp"], par["kexp"],
-              CN_STEEPNESS, CN_CUTOFF, REPULSION_CUTOFF, INTEGRAL_CUTOFF, par["gexp"]]
+    g[:15] = [par["kpol"], par["enscale"], sh["ss"], sh["pp"], sh["dd"], sh["sp"], par["kexp"],
+              CN_STEEPNESS, CN_CUTOFF, REPULSION_CUTOFF, INTEGRAL_CUTOFF, par["gexp"],
+              par["halogen"]["damping"], par["halogen"]["rscale"], XB_CUTOFF]
     return Tables(
         elem_shell0=elem_shell0, elem_nshell=elem_nshell, elem_data=np.ascontiguousarray(elem_data),
         shell_int=np.ascontiguousarray(np.asarray(shell_int, dtype=np.int32)),

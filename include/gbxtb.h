@@ -50,19 +50,24 @@ extern "C" {
                                      (reference raises, wavefunction/filling.py:366) */
 #define GBXTB_MOL_CHOLESKY_FAIL 4 /* overlap not positive definite */
 #define GBXTB_MOL_NONFINITE 8     /* NaN/Inf appeared */
+#define GBXTB_MOL_RESTARTED 16    /* not a failure: the molecule did not converge in
+                                     opts->restart_at passes and was solved again
+                                     from the guess with the reference's Anderson
+                                     mixer (iterations count that second run) */
 
 typedef struct gbxtb_ctx gbxtb_ctx;
 typedef struct gbxtb_plan gbxtb_plan;
 
 /* Number of doubles per element / shell record in gbxtb_params. */
-#define GBXTB_ELEM_DOUBLES 8   /* gam, gam3, zeff, arep, en, rad(bohr), rcov_d3(bohr), 0 */
+#define GBXTB_ELEM_DOUBLES 8   /* gam, gam3, zeff, arep, en, rad(bohr), rcov_d3(bohr), xbond */
 #define GBXTB_SHELL_INTS 4     /* l, nprim, valence, 0 */
 #define GBXTB_SHELL_DOUBLES 24 /* alpha[8], coeff[8], level(Eh), kcn(Eh), shpoly, refocc, lgam, 0, 0, 0 */
 #define GBXTB_MAX_PRIM 8
 #define GBXTB_GLOBALS 16
 /* globals: 0 kpol, 1 enscale, 2 k_ss, 3 k_pp, 4 k_dd, 5 k_sp, 6 kexp (repulsion),
  *          7 cn steepness, 8 cn cutoff, 9 repulsion cutoff, 10 integral cutoff,
- *          11 gexp (must be 2), 12..15 unused */
+ *          11 gexp (must be 2), 12 halogen-bond damping, 13 halogen-bond radius
+ *          scale, 14 halogen-bond cutoff (bohr), 15 unused */
 
 /* GFN1 parameter tables (host).  Element z uses shell records
  * [elem_shell0[z], elem_shell0[z] + elem_nshell[z]).  Contraction
@@ -118,12 +123,22 @@ typedef struct {
                               (scf/unrolling/default.py:92-96) */
   int32_t damp_dynamic;    /* 1: once the potential change is below 0.1, later
                               steps use damp_dynamic_factor ("damp_dynamic", 0) */
-  int32_t reserved;        /* 0 */
+  int32_t no_halogen;      /* 1: without the halogen-bond term (reference option
+                              exclude=["hal"]); 0: with it (the default) */
   double damp_dynamic_factor; /* ("damp_dynamic_factor", 0.99) */
   double fermi_thresh;     /* |sum f - n| at which the Fermi-level Newton search
                               stops ("fermi_thresh"); <= 0: sqrt(machine eps),
                               the reference's default (wavefunction/filling.py:
                               269-366) */
+  int32_t restart_at;      /* with the Broyden or simple mixer: a molecule still
+                              iterating after this many passes starts again from
+                              the guess with the reference's Anderson mixer
+                              (generations, damp, damp_init, diagonal_offset,
+                              soft_start above), every pass in FP64, with a fresh
+                              maxiter budget, so that it follows the reference's
+                              own SCF where the faster mixer does not converge;
+                              0: never */
+  int32_t reserved;        /* 0 */
 } gbxtb_options;
 
 /* The reference's default SCF options (calculators/config/scf.py:139-190,

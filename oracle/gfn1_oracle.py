@@ -81,6 +81,13 @@ COV_D3 = np.array([0.0] + _COV_D3) * (4.0 / 3.0) * AA2AU
 # Cartesian -> real spherical transformation, rows in the reference's
 # ordering (integral/driver/pytorch/impls/md/trafo.py:63-90, NLM_CART 165-182).
 _S3 = math.sqrt(3.0)
+# The reference keeps its double factorials (basis/slater.py:53-55) and this
+# table in float32 tensors, so its d shells are normalised with
+# 1/float32(sqrt(3)) and the xy-type rows carry float32(sqrt(3)): those two
+# roundings cancel, but the d_z2 row (-xx/2 - yy/2 + zz) keeps a factor
+# sqrt(3)/float32(sqrt(3)) = 1 + 1.8e-8, which shows in every integral and
+# energy of a molecule with d shells.  It is reproduced here.
+DZ2_SCALE = _S3 / float(np.float32(np.sqrt(np.float32(3.0))))
 CART = {
     0: [(0, 0, 0)],
     1: [(1, 0, 0), (0, 1, 0), (0, 0, 1)],
@@ -90,7 +97,7 @@ TRAFO = {
     0: np.array([[1.0]]),
     1: np.array([[0.0, 1.0, 0.0], [0.0, 0.0, 1.0], [1.0, 0.0, 0.0]]),  # (y, z, x)
     2: np.array([
-        [-0.5, -0.5, 1.0, 0.0, 0.0, 0.0],
+        [-0.5 * DZ2_SCALE, -0.5 * DZ2_SCALE, DZ2_SCALE, 0.0, 0.0, 0.0],
         [0.0, 0.0, 0.0, 0.0, _S3, 0.0],
         [0.0, 0.0, 0.0, 0.0, 0.0, _S3],
         [0.5 * _S3, -0.5 * _S3, 0.0, 0.0, 0.0, 0.0],
@@ -433,6 +440,67 @@ def repulsion(numbers, positions, grad: bool = False):
     return eat, g
 
 
+XB_DONORS = (17, 35, 53, 85)       # components/classicals/halogen/hal.py:117
+XB_ACCEPTORS = (7, 8, 15, 16)      # hal.py:118
+XB_CUTOFF = 20.0                   # constants/xtb.py:33
+
+
+def halogen_bond(numbers, positions, grad: bool = False):
+    """GFN1 halogen-bond correction (classicals/halogen/hal.py:168-364).
+    Triples (X, J, K): donor X, acceptor J within the cutoff (hal.py:213-226)
+    and the atom K nearest to X at a non-zero distance, first of equals
+    (hal.py:235-246).  E_X += xbond_X lj fdamp with lj = (s^12 - damp s^6) /
+    (1 + s^12), s = rscale (R_X + R_J) / R_XJ and fdamp = (0.5 - 0.25
+    cosa)^6, cosa = (d_XK^2 + d_XJ^2 - d_KJ^2) / (d_XK d_XJ) (hal.py:
+    321-359).  The gradient is that expression differentiated by hand."""
+    par = params()
+    hal = par["halogen"]
+    numbers = np.asarray(numbers)
+    pos = np.asarray(positions, dtype=np.float64)
+    n = len(numbers)
+    eat = np.zeros(n)
+    g = np.zeros((n, 3))
+    rads = ATOMIC_RADII[numbers] * hal["rscale"]
+    for x in range(n):
+        zx = int(numbers[x])
+        if zx not in XB_DONORS:
+            continue
+        xb = par["elements"][str(zx)].get("xbond", 0.0)
+        # nearest neighbour of the donor (hal.py:235-246)
+        k, dist = 0, np.finfo(np.float64).max
+        for b in range(n):
+            r1 = float(np.linalg.norm(pos[x] - pos[b]))
+            if 0.0 < r1 < dist:
+                k, dist = b, r1
+        for j in range(n):
+            if int(numbers[j]) not in XB_ACCEPTORS or np.linalg.norm(pos[x] - pos[j]) > XB_CUTOFF:
+                continue
+            u, v = pos[j] - pos[x], pos[k] - pos[x]
+            d2xj, d2xk, d2kj = u @ u, v @ v, (pos[k] - pos[j]) @ (pos[k] - pos[j])
+            rxj = np.sqrt(d2xj)
+            s = (rads[x] + rads[j]) / rxj
+            s6 = s ** 6
+            s12 = s6 * s6
+            lj = (s12 - hal["damping"] * s6) / (1.0 + s12)
+            cosa = (d2xk + d2xj - d2kj) / np.sqrt(d2xk * d2xj)
+            h = 0.5 - 0.25 * cosa
+            eat[x] += xb * lj * h ** 6
+            if grad:
+                rv = np.sqrt(d2xk)
+                c = 0.5 * cosa  # cosine of the angle J-X-K
+                dlj = -(12 * s12 - 6 * hal["damping"] * s6 + 6 * hal["damping"] * s6 * s12) / (
+                    rxj * (1.0 + s12) ** 2)
+                dfd = -3.0 * h ** 5  # d h^6 / d c, with h = 0.5 - 0.5 c
+                dcdu = v / (rxj * rv) - c * u / d2xj
+                dcdv = u / (rxj * rv) - c * v / d2xk
+                du = xb * (dlj * u / rxj * h ** 6 + lj * dfd * dcdu)
+                dv = xb * lj * dfd * dcdv
+                g[j] += du
+                g[k] += dv
+                g[x] -= du + dv
+    return (eat, g) if grad else eat
+
+
 # ---------------------------------------------------------------------------
 # SCF pieces
 # ---------------------------------------------------------------------------
@@ -612,11 +680,15 @@ def singlepoint(numbers, positions, chrg: float = 0.0, spin=None, forces: bool =
     par = params()
     kt = etemp * KELVIN2AU
 
-    # classical repulsion
+    # classical terms: repulsion and halogen bond
     if forces:
         erep_at, grad_rep = repulsion(numbers, positions, grad=True)
+        exb_at, grad_xb = halogen_bond(numbers, positions, grad=True)
+        grad_rep = grad_rep + grad_xb
     else:
         erep_at = repulsion(numbers, positions)
+        exb_at = halogen_bond(numbers, positions)
+    erep_at = erep_at + exb_at
 
     # integrals
     if forces:

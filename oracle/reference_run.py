@@ -117,3 +117,25 @@ def singlepoint(numbers, positions, chrg: float = 0.0, spin=None, forces: bool =
         pos2 = torch.as_tensor(np.asarray(positions), dtype=torch.float64).clone().requires_grad_(True)
         out["forces_analytical"] = calc2.forces_analytical(pos2, chrg=chrg, spin=spin).detach().numpy().copy()
     return out
+
+
+def halogen_energy(numbers, positions) -> tuple["np.ndarray", "np.ndarray"]:
+    """The reference's halogen-bond correction alone
+    (``components/classicals/halogen/hal.py:168-364``): per-atom energies
+    and the gradient of their sum (autograd), for a single molecule."""
+    _setup_path()
+    import numpy as np
+    import torch
+
+    from dxtb import GFN1_XTB, IndexHelper
+    from dxtb._src.components.classicals import new_halogen
+
+    num = torch.as_tensor(np.asarray(numbers), dtype=torch.int64)
+    pos = torch.as_tensor(np.asarray(positions), dtype=torch.float64).clone().requires_grad_(True)
+    xb = new_halogen(torch.unique(num), GFN1_XTB, dtype=torch.float64)
+    if xb is None:
+        return np.zeros(len(num)), np.zeros((len(num), 3))
+    cache = xb.get_cache(num, IndexHelper.from_numbers(num, GFN1_XTB))
+    e = xb.get_energy(pos, cache)
+    (g,) = torch.autograd.grad(e.sum(), pos)
+    return e.detach().numpy().copy(), g.numpy().copy()

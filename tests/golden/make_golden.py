@@ -13,7 +13,9 @@ Outputs (ragged arrays concatenated over molecules, ``offsets`` delimit them):
   (``test/test_singlepoint/mols/*/coord``);
 * ``synthetic.npz``: seeded synthetic CHNO molecules from
   ``dxtb_gb300.molgen`` (the 20-atom single-point molecule, molecules of the
-  10-120-atom batch workload and of the perturbed 30-60-atom force workload).
+  10-120-atom batch workload and of the perturbed 30-60-atom force workload);
+* ``halogen.npz`` (``--halogen``): synthetic molecules with Br/I
+  halogen-bond donors, with the reference's halogen-bond term alone as well.
 """
 from __future__ import annotations
 
@@ -92,7 +94,35 @@ def main(quick: bool) -> None:
     _pack(recs, names, HERE / "synthetic.npz")
 
 
+def main_halogen() -> None:
+    """``halogen.npz``: synthetic molecules with Br/I donors
+    (``dxtb_gb300.molgen.halogenated``), with the reference's full single
+    point (energy, charges, autograd forces) and its halogen-bond term alone
+    (``xb_energy`` per molecule, ``xb_gradient`` per atom)."""
+    if not rr.available():
+        raise SystemExit("reference source tree not found")
+    recs, names, xbe, xbg = [], [], [], []
+    for i, (nat, nhal) in enumerate([(12, 1), (20, 2), (24, 2), (30, 3), (40, 2), (50, 4)]):
+        num, pos = molgen.halogenated(nat, 9100 + i, nhal)
+        recs.append(run(num, pos, label=f"halogen-{i}"))
+        names.append(f"halogen-{i}")
+        e, g = rr.halogen_energy(num, pos)
+        xbe.append(float(e.sum()))
+        xbg.append(g)
+    _pack(recs, names, HERE / "halogen.npz")
+    g = dict(np.load(HERE / "halogen.npz"))
+    g["xb_energy"] = np.array(xbe)
+    g["xb_gradient"] = np.concatenate(xbg)
+    np.savez_compressed(HERE / "halogen.npz", **g)
+    print("halogen-bond energies", xbe)
+
+
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--quick", action="store_true")
-    main(ap.parse_args().quick)
+    ap.add_argument("--halogen", action="store_true", help="only halogen.npz")
+    a = ap.parse_args()
+    if a.halogen:
+        main_halogen()
+    else:
+        main(a.quick)

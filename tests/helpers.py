@@ -42,18 +42,25 @@ def restart_energy(numbers, positions, v_orbital):
     return bool(r.converged), int(r.iterations), float(r.energy)
 
 
-def fd_force_component(numbers, positions, atom, axis, h=5e-4):
+def fd_force_component(numbers, positions, atom, axis, v_orbital, h=2e-4):
     """Five-point central difference (truncation error O(h^4)) of the oracle
-    energy: the force component -dE/dR[atom, axis].  The electron count is
-    solved to 1e-13, since at the reference's sqrt(eps) Fermi tolerance the
-    energy carries ~5e-9 Eh of noise (5e-6 Eh/bohr after dividing by h)."""
+    energy: the force component -dE/dR[atom, axis].  Every displaced SCF
+    starts from the converged orbital potential of the undisplaced geometry,
+    so that it stays on the same SCF solution (molecules with several
+    solutions would otherwise mix branches), and is converged to 1e-12 with
+    the electron count solved to 1e-13: at the reference's sqrt(eps) Fermi
+    tolerance the energy carries ~5e-9 Eh of noise."""
     from oracle import gfn1_oracle as go
 
     e = {}
     for st in (-2, -1, 1, 2):
         p = np.array(positions, dtype=np.float64, copy=True)
         p[atom, axis] += st * h
-        e[st] = go.singlepoint(numbers, p, mixer="broyden", forces=False, fermi_thr=1e-13).energy
+        r = go.singlepoint(numbers, p, mixer="broyden", forces=False, fermi_thr=1e-13, v_init=v_orbital,
+                           x_atol=1e-12, x_atol_max=1e-12, maxiter=200)
+        if not r.converged:
+            return float("nan")
+        e[st] = r.energy
     return -(8.0 * (e[1] - e[-1]) - (e[2] - e[-2])) / (12.0 * h)
 
 

@@ -49,3 +49,31 @@ def test_clock_summary_parses_nvidia_smi_rows(tmp_path):
     s = clk.summary()
     assert s["sm_mhz"] == 2070.0 and s["sm_max_mhz"] == 2070.0
     assert s["reasons"] == ["sw_power_cap"] and s["samples"] == 3
+
+
+def test_size_matched_sample_spans_the_size_range():
+    mols = [(np.ones(n, dtype=int), None) for n in [50, 10, 120, 30, 70, 90, 11, 119]]
+    idx = bench.size_matched(mols, 4)
+    sizes = [len(mols[i][0]) for i in idx]
+    assert sizes == sorted(sizes) and sizes[0] == 10 and sizes[-1] == 120
+    assert len(set(idx)) == 4
+
+
+def test_parity_summary_classifies_every_molecule():
+    class R:
+        pass
+
+    import torch
+
+    r = R()
+    r.energy = torch.tensor([1.0, 2.0 + 5e-9, 3.5, 4.0 + 1e-6, 5.0, 6.0])
+    r.status = np.array([0, 0, 0, 0, 1, 0])
+    r.iterations = np.array([10, 11, 12, 13, 301, 14])
+    r.fp32_passes = np.zeros(6, dtype=int)
+    ref = {"energy": np.array([1.0, 2.0, 3.0, 4.0, 5.0, 6.0]),
+           "converged": np.array([True, True, True, True, True, False]),
+           "iterations": np.array([10, 12, 12, 13, 20, 301])}
+    p = bench.parity_summary(r, ref, seconds=2.0)
+    assert p["verified"] == 2 and p["other_state"] == 1 and p["imprecise"] == 1
+    assert p["reference_only_converged"] == 1 and p["both_converged"] == 4
+    assert p["verified_rate"] == 1.0 and p["iterations_equal_to_reference"] == 1

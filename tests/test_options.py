@@ -36,6 +36,7 @@ def test_mixer_options_reach_the_engine():
     ({"no_such_option": 1}, ValueError),
     ({"exclude": []}, ValueError),
     ({"exclude": ["disp", "es3"]}, NotImplementedError),
+    ({"exclude": ["disp", "rep"]}, NotImplementedError),
 ])
 def test_unsupported_options_raise(opts, err):
     with pytest.raises(err):
@@ -46,3 +47,10 @@ def test_options_without_numerical_effect_are_accepted():
     o = resolve_opts({**BASE, "scf_mode": "implicit", "int_driver": "pytorch", "batch_mode": 1,
                       "f_atol": 1e-6, "verbosity": 0})
     assert o["mixer"] == "broyden"
+
+
+def test_halogen_bond_switch():
+    assert engine_options(resolve_opts(BASE), False).no_halogen == 0
+    assert engine_options(resolve_opts({"exclude": ["disp", "hal"]}), False).no_halogen == 1
+    # GFN2-only terms are absent from GFN1 anyway
+    assert engine_options(resolve_opts({"exclude": ["disp", "aes2", "d4sc"]}), False).no_halogen == 0

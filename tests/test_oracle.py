@@ -69,3 +69,29 @@ def test_finite_difference_forces():
             e1 = go.singlepoint(num, p1, forces=False).energy
             e2 = go.singlepoint(num, p2, forces=False).energy
             assert abs(-(e1 - e2) / (2 * h) - r.forces[a, x]) < 1e-7
+
+
+def test_halogen_bond_term_against_reference():
+    """The oracle's halogen-bond term (energy and hand-derived gradient)
+    against the reference's own term and its autograd gradient
+    (tests/golden/halogen.npz, classicals/halogen/hal.py:168-364)."""
+    from tests.helpers import GOLDEN
+
+    g = np.load(GOLDEN / "halogen.npz")
+    offs = g["offsets"]
+    for k in range(len(offs) - 1):
+        a, b = offs[k], offs[k + 1]
+        e, grad = go.halogen_bond(g["numbers"][a:b], g["positions"][a:b], grad=True)
+        assert abs(e.sum() - g["xb_energy"][k]) < 1e-14
+        assert np.abs(grad - g["xb_gradient"][a:b]).max() < 1e-13
+    assert np.abs(g["xb_energy"]).max() > 1e-2  # the set has a sizeable halogen bond
+
+
+@pytest.mark.parametrize("mol", load_golden("halogen.npz"), ids=lambda m: m["name"])
+def test_halogenated_molecules(mol):
+    """Whole single points with Br/I donors: oracle == reference."""
+    r = go.singlepoint(mol["numbers"], mol["positions"], chrg=mol["charge"])
+    assert r.converged
+    assert abs(r.energy - mol["energy"]) < E_TOL
+    assert np.abs(r.charges - mol["charges"]).max() < Q_TOL
+    assert np.abs(r.forces - mol["forces"]).max() < 1e-6
