@@ -380,3 +380,30 @@ def test_large_molecule_against_oracle():
     assert r64.status[0] == 0
     assert abs(r64.energy.item() - r.energy) < E_TOL
     assert np.abs(-r64.gradient.cpu().numpy() - r.forces).max() < F_TOL
+
+
+def test_halogenated_molecules_against_reference():
+    """Molecules with Br/I halogen-bond donors (tests/golden/halogen.npz,
+    produced by the reference): energies 1e-8 Eh, charges 1e-7 e, forces
+    1e-6 Eh/bohr.  The halogen-bond term is classical, so switching it off
+    (exclude "hal") changes the energy by exactly the reference's term and
+    the gradient by exactly its gradient."""
+    mols = load_golden("halogen.npz")
+    g = np.load(GOLDEN / "halogen.npz")
+    num, pos = pad([(m["numbers"], m["positions"]) for m in mols])
+    p = torch.tensor(pos, device="cuda")
+    res = calc_for(num, mixer="anderson", mixed_precision=False).singlepoint(p, forces=True)
+    off_ = calc_for(num, mixer="anderson", mixed_precision=False, exclude=["disp", "hal"]).singlepoint(
+        p, forces=True)
+    e, q, f = res.energy.cpu().numpy(), res.charges.cpu().numpy(), -res.gradient.cpu().numpy()
+    e0, f0 = off_.energy.cpu().numpy(), -off_.gradient.cpu().numpy()
+    off = 0
+    for k, m in enumerate(mols):
+        n = len(m["numbers"])
+        assert res.status[k] == 0, m["name"]
+        assert abs(e[k] - m["energy"]) < E_TOL, m["name"]
+        assert np.abs(q[off:off + n] - m["charges"]).max() < Q_TOL, m["name"]
+        assert np.abs(f[off:off + n] - m["forces"]).max() < F_TOL, m["name"]
+        assert abs((e[k] - e0[k]) - g["xb_energy"][k]) < 1e-12, m["name"]
+        assert np.abs((f0 - f)[off:off + n] - g["xb_gradient"][off:off + n]).max() < 1e-12, m["name"]
+        off += n
