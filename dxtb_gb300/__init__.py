@@ -8,7 +8,7 @@ from __future__ import annotations
 
 __version__ = "0.1.0"
 
-__all__ = ["GFN1Calculator", "SCFConvergenceWarning", "SCFConvergenceError", "build"]
+__all__ = ["GFN1Calculator", "SCFConvergenceWarning", "SCFConvergenceError", "build", "io"]
 
 
 def __getattr__(name):
@@ -20,4 +20,8 @@ def __getattr__(name):
         from .build import build
 
         return build
+    if name == "io":
+        import importlib
+
+        return importlib.import_module(f"{__name__}.io")
     raise AttributeError(name)

@@ -209,6 +209,15 @@ class Server:
         self.queue.append(req)
         return req
 
+    def submit_file(self, path, t_submit: float | None = None) -> Request:
+        """Queue one single point read from a ``coord`` or ``xyz`` file, with
+        the charge and unpaired electrons of the ``.CHRG`` / ``.UHF`` files
+        beside it (``dxtb_gb300.io.read_molecule``)."""
+        from .io import read_molecule
+
+        mol = read_molecule(path)
+        return self.submit(mol["numbers"], mol["positions"], mol["charge"], mol["uhf"], t_submit)
+
     def _admit(self) -> None:
         waiting = deque()
         while self.queue:
