@@ -531,10 +531,10 @@ int enqueue_pass(gbxtb_plan *plan, const Work &w, const gbxtb_options &o, bool t
   prof.end(GBXTB_PROF_FOCK, 1);
   prof.begin(GBXTB_PROF_TRIDIAG);
   // FP32 passes in shared memory, except large molecules in the tail
-  if (opts->mixed_precision) launch_tridiag_smem(pl, w, s);
+  if (opts->mixed_precision) launch_tridiag_smem(pl, w, s, tail);
   int ntrd = opts->mixed_precision ? plan->smem_launches : 0;
   if (tail) {
-    ntrd += launch_tridiag_cluster(pl, w, w.active_list, active, plan->maxn, s);
+    ntrd += launch_tridiag_cluster(pl, w, w.active_list, active, plan->maxn, s, true);
   } else {
     // large FP64 passes and FP32 passes too large for shared memory on 8-SM
     // clusters, the rest one CTA per molecule

@@ -41,6 +41,10 @@ constexpr int kClusterMinN = 128;
 // Cluster passes of molecules with more AOs than this use the blocked
 // (panel) cluster tridiagonalisation; smaller ones the column-by-column one.
 constexpr int kClusterBlockedMinN = 400;
+// In the tail of a batch (fewer molecules than SMs), FP32 passes of
+// molecules with more AOs than this tridiagonalise on an 8-SM cluster with
+// the matrix in the cluster's shared memory instead of on one SM.
+constexpr int kTailClusterMinN = 160;
 
 // Passes that tridiagonalise on an 8-SM cluster in every pass (not only in
 // the tail of a batch): FP64 passes above kClusterMinN AOs and FP32 passes

@@ -492,12 +492,13 @@ constexpr int kSmemCols = (kSmemLocalMaxN + 31) / 32;  // column slots per lane
 
 // NW warps per CTA (the size class picks it: more warps for larger molecules)
 template <int NW>
-__global__ void __launch_bounds__(NW * 32) k_tridiag_smem(DevPlan pl, Work w, const int32_t *mol_list) {
+__global__ void __launch_bounds__(NW * 32) k_tridiag_smem(DevPlan pl, Work w, const int32_t *mol_list, int tail) {
   constexpr int kSmemWarps = NW;
   const int m = mol_list[blockIdx.x];
   if (w.phase[m] == kPhaseDone || w.prec[m] != 0) return;
   const MolDesc md = pl.mol[m];
   const int n = md.nao;
+  if (tail && n > kTailClusterMinN) return;  // on a cluster (k_tridiag_cluster)
   const int k0 = n > kSmemLocalMaxN ? n - kSmemLocalMaxN : 0;  // steps in global memory
   const int nl = n - k0;                                        // trailing size on chip
   extern __shared__ float smf[];
@@ -714,13 +715,10 @@ __global__ void __launch_bounds__(NW * 32) k_tridiag_smem(DevPlan pl, Work w, co
 // Householder tridiagonalisation on a thread-block cluster (8 SMs per
 // molecule), column by column, for molecules up to kClusterBlockedMinN AOs:
 // FP64 passes above kClusterMinN AOs, and every pass in the tail of a batch,
-// when one SM per molecule would leave the GPU idle.  Rows are owned cyclically (row i by CTA
-// i mod 8); every CTA rebuilds the reflector from the column in L2, forms
-// p = tau A v and the rank-2 update for its own rows, and the two global
-// quantities of a step (p.v and the vector w) are exchanged through
-// distributed shared memory between three cluster barriers.  Matrix reads
-// bypass L1 (ld.global.cg) since other SMs of the cluster write the rows.
-// Same arithmetic and storage conventions as k_tridiag.
+// when one SM per molecule would leave the GPU idle.  The matrix lives in
+// the cluster's shared memory for the whole reduction (rows owned
+// cyclically, row i by CTA i mod 8; tridiag_cluster_onchip below).  Same
+// arithmetic and storage conventions as k_tridiag.
 // ---------------------------------------------------------------------------
 constexpr int kClusterSize = 8;
 constexpr int kTrdClThreads = 256;
@@ -730,26 +728,73 @@ __device__ __forceinline__ T ld_cg(const T *p) {
   return __ldcg(p);
 }
 
+// The same reduction with the matrix held on chip: the 8 CTAs of the
+// cluster keep their own rows (row i on CTA i mod 8, full length n) in
+// shared memory for the whole tridiagonalisation, so that the matrix-vector
+// product and the rank-2 update of a step touch only local shared memory.
+// A step needs two cluster barriers:
+//   (a) every CTA sums the eight partial norms of column k published before
+//       the previous barrier, reads alpha from the owner of row k+1 and
+//       builds the reflector from the owners' column entries (distributed
+//       shared memory); (b) p = tau A22 v for its own rows and the partial
+//       p.v are published;  -- barrier 1 --
+//   (c) every CTA sums the partials, gathers p from the owners and forms
+//       w = p - tau/2 (p.v) v for all rows; (d) A22 -= v w^T + w v^T on its
+//       own rows, with the partial norm of column k+1 accumulated on the
+//       fly and published.  -- barrier 2 --
+// Every CTA computes tau, beta and the scale from the same eight partials
+// in the same order, so every branch on them is uniform over the cluster.
+// Partial norms and p.v partials are double-buffered by the parity of k: a
+// buffer is rewritten only after a barrier that follows its last read.
+// Output conventions as tridiag_body (reflector k in row k of A in global
+// memory, d, e, tau).
 template <typename T>
-__device__ __forceinline__ void tridiag_cluster_unblocked(cg::cluster_group &cluster, const MolDesc &md,
-                                                     const Work &w, T *sm, T *red, T *kpart) {
+__device__ __forceinline__ void tridiag_cluster_onchip(cg::cluster_group &cluster, const MolDesc &md,
+                                                       const Work &w, T *sm, T *red, T *nrm2, T *kp2) {
   const int rank = (int)cluster.block_rank();
   const int n = md.nao;
-  T *A = mat_view<T>(w.A, md.mat0);
+  const int nloc = (n - rank + kClusterSize - 1) / kClusterSize;  // rows rank, rank + 8, ...
+  T *Ag = mat_view<T>(w.A, md.mat0);
   double *d = w.d + md.ao0, *e = w.e + md.ao0, *tau = w.tau + md.ao0;
-  T *vs = sm;          // [n] full reflector
-  T *ws = sm + n;      // [n] p, then w, for own rows; full w after gather
+  T *rows = sm;                                   // [nloc_max][n]
+  const int nloc_max = (n + kClusterSize - 1) / kClusterSize;
+  T *vs = rows + (size_t)nloc_max * n;            // [n] reflector
+  T *wv = vs + n;                                 // [n] w of all rows
+  T *ps = wv + n;                                 // [nloc_max] p of own rows (read by all)
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  // element (i, j) of the matrix in its owner's shared memory
+  auto remote = [&](int i, int j) -> T {
+    const T *base = cluster.map_shared_rank(rows, i % kClusterSize);
+    return base[(size_t)(i / kClusterSize) * n + j];
+  };
+  // load own rows
+  for (int li = wid; li < nloc; li += nw) {
+    const T *src = Ag + (int64_t)(rank + li * kClusterSize) * n;
+    T *dst = rows + (size_t)li * n;
+    for (int j = lane; j < n; j += 32) dst[j] = src[j];
+  }
+  __syncthreads();
+  // partial norm of column 0 over own rows i >= 2
+  {
+    T part = T(0);
+    for (int li = threadIdx.x; li < nloc; li += blockDim.x) {
+      const int i = rank + li * kClusterSize;
+      if (i >= 2) {
+        const T x = rows[(size_t)li * n];
+        part += x * x;
+      }
+    }
+    part = block_sum(part, red);
+    if (threadIdx.x == 0) nrm2[0] = part;
+  }
+  cluster.sync();
   for (int k = 0; k + 2 < n; ++k) {
     const int m1 = n - k - 1;
-    // column x = A[k+1.., k] (rebuilt redundantly by every CTA)
-    T part = T(0);
-    for (int t = 1 + threadIdx.x; t < m1; t += blockDim.x) {
-      const T x = ld_cg(A + (int64_t)(k + 1 + t) * n + k);
-      part += x * x;
-    }
-    const T xn2 = block_sum(part, red);
-    const T alpha = ld_cg(A + (int64_t)(k + 1) * n + k);
+    const int buf = k & 1;
+    // (a) reflector
+    T xn2 = T(0);
+    for (int r = 0; r < kClusterSize; ++r) xn2 += cluster.map_shared_rank(nrm2, r)[buf];
+    const T alpha = remote(k + 1, k);
     T tk = T(0), scale = T(0), beta = alpha;
     if (xn2 != T(0)) {
       beta = -copysign(sqrt(alpha * alpha + xn2), alpha);
@@ -757,91 +802,115 @@ __device__ __forceinline__ void tridiag_cluster_unblocked(cg::cluster_group &clu
       scale = T(1) / (alpha - beta);
     }
     if (rank == 0 && threadIdx.x == 0) {
-      d[k] = ld_cg(A + (int64_t)k * n + k);
+      d[k] = remote(k, k);
       e[k] = beta;
       tau[k] = tk;
     }
+    // first own row at or after k + 1
+    const int lfirst = (k + 1 - rank + kClusterSize - 1) / kClusterSize > 0
+                           ? (k + 1 - rank + kClusterSize - 1) / kClusterSize : 0;
     if (tk == T(0)) {
+      // no reflection: publish the partial norm of column k + 1 and go on
+      T part = T(0);
+      for (int li = lfirst + threadIdx.x; li < nloc; li += blockDim.x) {
+        const int i = rank + li * kClusterSize;
+        if (i >= k + 3) {
+          const T x = rows[(size_t)li * n + k + 1];
+          part += x * x;
+        }
+      }
+      part = block_sum(part, red);
+      if (threadIdx.x == 0) nrm2[buf ^ 1] = part;
       cluster.sync();
       continue;
     }
-    for (int t = threadIdx.x; t < m1; t += blockDim.x)
-      vs[t] = (t == 0) ? T(1) : ld_cg(A + (int64_t)(k + 1 + t) * n + k) * scale;
+    for (int t = threadIdx.x; t < m1; t += blockDim.x) vs[t] = (t == 0) ? T(1) : remote(k + 1 + t, k) * scale;
     __syncthreads();
     if (rank == 0)
-      for (int t = threadIdx.x; t < m1; t += blockDim.x) A[(int64_t)k * n + k + 1 + t] = vs[t];
-    // p = tau A22 v for own rows (warp per row)
-    const int first = (rank - (k + 1) % kClusterSize + kClusterSize) % kClusterSize;
+      for (int t = threadIdx.x; t < m1; t += blockDim.x) Ag[(int64_t)k * n + k + 1 + t] = vs[t];
+    // (b) p = tau A22 v for own rows (warp per row), partial p.v
     T pv = T(0);
-    for (int t0 = wid; ; t0 += nw) {
-      // own rows: global row i = k+1+t with i % C == rank
-      const int t = first + t0 * kClusterSize;
-      if (t >= m1) break;
-      const T *row = A + (int64_t)(k + 1 + t) * n + (k + 1);
-      T sacc = T(0);
-      for (int j = lane; j < m1; j += 32) sacc += ld_cg(row + j) * vs[j];
-      sacc = warp_sum(sacc) * tk;
+    for (int li = lfirst + wid; li < nloc; li += nw) {
+      const int t = rank + li * kClusterSize - (k + 1);
+      const T *row = rows + (size_t)li * n + (k + 1);
+      T acc = T(0);
+      for (int j = lane; j < m1; j += 32) acc += row[j] * vs[j];
+      acc = warp_sum(acc) * tk;
       if (lane == 0) {
-        ws[t] = sacc;
-        pv += sacc * vs[t];
+        ps[li] = acc;
+        pv += acc * vs[t];
       }
     }
-    const T kp = block_sum(pv, red);
-    if (threadIdx.x == 0) *kpart = kp;
+    pv = block_sum(pv, red);
+    if (threadIdx.x == 0) kp2[buf] = pv;
     cluster.sync();
+    // (c) w for all rows
     T K = T(0);
-    for (int r = 0; r < kClusterSize; ++r) K += *cluster.map_shared_rank(kpart, r);
+    for (int r = 0; r < kClusterSize; ++r) K += cluster.map_shared_rank(kp2, r)[buf];
     const T half = T(0.5) * tk * K;
-    for (int t = first + threadIdx.x * kClusterSize; t < m1; t += blockDim.x * kClusterSize)
-      ws[t] -= half * vs[t];
-    cluster.sync();
-    // gather w of all rows into local shared memory
-    T *wl = sm + 2 * n;  // [n]
     for (int t = threadIdx.x; t < m1; t += blockDim.x) {
-      const int owner = (k + 1 + t) % kClusterSize;
-      wl[t] = *cluster.map_shared_rank(ws + t, owner);
+      const int i = k + 1 + t;
+      const T p = cluster.map_shared_rank(ps, i % kClusterSize)[i / kClusterSize];
+      wv[t] = p - half * vs[t];
     }
     __syncthreads();
-    // A22 -= v w^T + w v^T on own rows
-    for (int t = first + wid * kClusterSize; t < m1; t += nw * kClusterSize) {
-      T *row = A + (int64_t)(k + 1 + t) * n + (k + 1);
-      const T vi = vs[t], wi = wl[t];
-      for (int j = lane; j < m1; j += 32) row[j] -= vi * wl[j] + wi * vs[j];
+    // (d) rank-2 update of own rows, partial norm of column k + 1
+    T part = T(0);
+    for (int li = lfirst + wid; li < nloc; li += nw) {
+      const int t = rank + li * kClusterSize - (k + 1);
+      T *row = rows + (size_t)li * n + (k + 1);
+      const T vi = vs[t], wi = wv[t];
+      for (int j = lane; j < m1; j += 32) {
+        const T a = row[j] - (vi * wv[j] + wi * vs[j]);
+        row[j] = a;
+        if (j == 0 && t >= 2) part += a * a;  // column k + 1, rows k + 3 ...
+      }
     }
+    part = block_sum(part, red);
+    if (threadIdx.x == 0) nrm2[buf ^ 1] = part;
     cluster.sync();
   }
   if (rank == 0 && threadIdx.x == 0) {
     if (n >= 2) {
-      d[n - 2] = ld_cg(A + (int64_t)(n - 2) * n + (n - 2));
-      d[n - 1] = ld_cg(A + (int64_t)(n - 1) * n + (n - 1));
-      e[n - 2] = ld_cg(A + (int64_t)(n - 1) * n + (n - 2));
+      d[n - 2] = remote(n - 2, n - 2);
+      d[n - 1] = remote(n - 1, n - 1);
+      e[n - 2] = remote(n - 1, n - 2);
     } else {
-      d[0] = ld_cg(A);
+      d[0] = remote(0, 0);
     }
   }
 }
 
+// Shared memory of tridiag_cluster_onchip for n AOs.
+template <typename T>
+__host__ __device__ constexpr size_t onchip_smem_bytes(int n) {
+  return sizeof(T) * ((size_t)((n + kClusterSize - 1) / kClusterSize) * (n + 1) + 2 * (size_t)n);
+}
+
 __global__ void __cluster_dims__(kClusterSize, 1, 1) __launch_bounds__(kTrdClThreads)
-    k_tridiag_cluster(DevPlan pl, Work w, const int32_t *mol_list) {
+    k_tridiag_cluster(DevPlan pl, Work w, const int32_t *mol_list, int tail) {
   cg::cluster_group cluster = cg::this_cluster();
   const int m = list_mol(w, mol_list, blockIdx.x / kClusterSize);
   if (m < 0) return;  // the whole cluster
   const MolDesc md = pl.mol[m];
   extern __shared__ double sm[];
   __shared__ double red[32];
-  __shared__ double kpart;
+  __shared__ double nrm2[2], kp2[2];
   // uniform over the cluster; FP32 passes of molecules that fit in shared
-  // memory run in k_tridiag_smem, molecules above kClusterBlockedMinN AOs in
+  // memory run in k_tridiag_smem (in the tail of a batch only those up to
+  // kTailClusterMinN AOs), molecules above kClusterBlockedMinN AOs in
   // k_tridiag_cluster_blocked
-  const bool done = (w.phase[m] == kPhaseDone) || (w.prec[m] == 0 && md.nao <= kSmemTridiagMaxN) ||
-                    md.nao > kClusterBlockedMinN;
+  const bool smem32 = w.prec[m] == 0 && md.nao <= kSmemTridiagMaxN && !(tail && md.nao > kTailClusterMinN);
+  const bool done = (w.phase[m] == kPhaseDone) || smem32 || md.nao > kClusterBlockedMinN;
   if (!done) {
     if (w.prec[m])
-      tridiag_cluster_unblocked<double>(cluster, md, w, sm, red, &kpart);
+      tridiag_cluster_onchip<double>(cluster, md, w, sm, red, nrm2, kp2);
     else
-      tridiag_cluster_unblocked<float>(cluster, md, w, reinterpret_cast<float *>(sm),
-                                       reinterpret_cast<float *>(red), reinterpret_cast<float *>(&kpart));
+      tridiag_cluster_onchip<float>(cluster, md, w, reinterpret_cast<float *>(sm),
+                                    reinterpret_cast<float *>(red), reinterpret_cast<float *>(nrm2),
+                                    reinterpret_cast<float *>(kp2));
   }
+  // no CTA leaves while others may still read its shared memory
   cluster.sync();
 }
 
@@ -1837,17 +1906,17 @@ size_t tridiag_smem_bytes(int nmax, int nwarps) {
   return sizeof(float) * ((size_t)nloc * (nloc + 1) / 2 + 5 * (size_t)nmax + (size_t)nwarps * nloc);
 }
 
-void launch_tridiag_smem(const DevPlan &pl, const Work &w, cudaStream_t s) {
+void launch_tridiag_smem(const DevPlan &pl, const Work &w, cudaStream_t s, bool tail) {
   for (int c = 0; c < kSmemBins; ++c) {
     if (pl.bin_count[c] <= 0) continue;
     const int nw = pl.bin_warps[c] ? pl.bin_warps[c] : kSmemBinWarps[c];
     const size_t smem = tridiag_smem_bytes(pl.bin_maxn[c], nw);
     if (nw == 8)
-      k_tridiag_smem<8><<<pl.bin_count[c], 256, smem, s>>>(pl, w, pl.bin_mols[c]);
+      k_tridiag_smem<8><<<pl.bin_count[c], 256, smem, s>>>(pl, w, pl.bin_mols[c], tail ? 1 : 0);
     else if (nw == 16)
-      k_tridiag_smem<16><<<pl.bin_count[c], 512, smem, s>>>(pl, w, pl.bin_mols[c]);
+      k_tridiag_smem<16><<<pl.bin_count[c], 512, smem, s>>>(pl, w, pl.bin_mols[c], tail ? 1 : 0);
     else
-      k_tridiag_smem<32><<<pl.bin_count[c], 1024, smem, s>>>(pl, w, pl.bin_mols[c]);
+      k_tridiag_smem<32><<<pl.bin_count[c], 1024, smem, s>>>(pl, w, pl.bin_mols[c], tail ? 1 : 0);
   }
 }
 
@@ -1855,10 +1924,10 @@ void launch_tridiag_smem(const DevPlan &pl, const Work &w, cudaStream_t s) {
 // Cluster tridiagonalisation for the molecules listed in mol_list (device).
 // Returns the number of launches.
 int launch_tridiag_cluster(const DevPlan &pl, const Work &w, const int32_t *mol_list, int count, int maxn,
-                           cudaStream_t s) {
+                           cudaStream_t s, bool tail) {
   if (count <= 0) return 0;
-  const size_t smem = sizeof(double) * 3 * (size_t)min(maxn, kClusterBlockedMinN);
-  k_tridiag_cluster<<<count * kClusterSize, kTrdClThreads, smem, s>>>(pl, w, mol_list);
+  const size_t smem = onchip_smem_bytes<double>(min(maxn, kClusterBlockedMinN));
+  k_tridiag_cluster<<<count * kClusterSize, kTrdClThreads, smem, s>>>(pl, w, mol_list, tail ? 1 : 0);
   if (maxn <= kClusterBlockedMinN) return 1;
   k_tridiag_cluster_blocked<<<count * kClusterSize, kTrdBlkThreads, tridiag_cluster_smem_bytes(maxn), s>>>(
       pl, w, mol_list);
@@ -1955,6 +2024,14 @@ cudaError_t set_linalg_smem_limits(int maxn) {
     e = cudaFuncSetAttribute(k_bisect, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need3);
     if (e != cudaSuccess) return e;
     cur3 = need3;
+  }
+  // the on-chip cluster tridiagonalisation (up to kClusterBlockedMinN AOs)
+  static size_t cur_o = 0;
+  const size_t need_o = onchip_smem_bytes<double>(maxn < kClusterBlockedMinN ? maxn : kClusterBlockedMinN);
+  if (need_o > opt_in && need_o > cur_o) {
+    e = cudaFuncSetAttribute(k_tridiag_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need_o);
+    if (e != cudaSuccess) return e;
+    cur_o = need_o;
   }
   if (maxn > kClusterBlockedMinN && need_c > cur_c) {
     e = cudaFuncSetAttribute(k_tridiag_cluster_blocked, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need_c);

@@ -448,9 +448,9 @@ int gbxtb_pool_step_launch(gbxtb_pool *pool, void *stream) {
     const int active = pool->active, nclus = pool->nclus;
     const bool tail = active <= plan->num_sms;
     launch_gemm(pl, w, plan->tile0, plan->ntile, 6, 0, s);
-    if (o.mixed_precision) launch_tridiag_smem(pl, w, s);
+    if (o.mixed_precision) launch_tridiag_smem(pl, w, s, tail);
     if (tail) {
-      launch_tridiag_cluster(pl, w, w.active_list, active, plan->maxn, s);
+      launch_tridiag_cluster(pl, w, w.active_list, active, plan->maxn, s, true);
       launch_bisect(pl, w, plan->maxn, o.kt, w.active_list, active, 32, s);
     } else {
       if (nclus > 0) launch_tridiag_cluster(pl, w, w.cluster_list, nclus, plan->maxn, s);

@@ -113,3 +113,74 @@ def test_blocked_model_zero_column():
     assert tau[0] == 0.0
     t = np.diag(d) + np.diag(e, 1) + np.diag(e, -1)
     assert np.abs(np.linalg.eigvalsh(t) - np.linalg.eigvalsh(m)).max() < 1e-12
+
+
+def onchip_cluster_tridiag(a: np.ndarray, csize: int = 8):
+    """Phase-by-phase model of tridiag_cluster_onchip (csrc/linalg.cu): rows
+    owned cyclically by `csize` CTAs in their shared memory, partial column
+    norms published per CTA (the norm of column k+1 accumulated during the
+    update of step k), p of own rows gathered by every CTA.  Returns d, e,
+    tau and the reflector rows, in the kernel's index conventions."""
+    n = a.shape[0]
+    own = [[i for i in range(n) if i % csize == r] for r in range(csize)]
+    rows = {i: a[i].copy() for i in range(n)}  # row i on CTA i % csize
+    d, e, tau = np.zeros(n), np.zeros(n), np.zeros(n)
+    refl = np.zeros((n, n))
+    nrm = [sum(rows[i][0] ** 2 for i in own[r] if i >= 2) for r in range(csize)]
+    for k in range(n - 2):
+        m1 = n - k - 1
+        xn2 = sum(nrm)
+        alpha = rows[k + 1][k]
+        tk, scale, beta = 0.0, 0.0, alpha
+        if xn2 != 0.0:
+            beta = -np.copysign(np.sqrt(alpha * alpha + xn2), alpha)
+            tk = (beta - alpha) / beta
+            scale = 1.0 / (alpha - beta)
+        d[k], e[k], tau[k] = rows[k][k], beta, tk
+        if tk == 0.0:
+            nrm = [sum(rows[i][k + 1] ** 2 for i in own[r] if i >= k + 3) for r in range(csize)]
+            continue
+        v = np.array([1.0] + [rows[k + 1 + t][k] * scale for t in range(1, m1)])
+        refl[k, k + 1:] = v
+        ps, kp = {}, [0.0] * csize
+        for r in range(csize):
+            for i in own[r]:
+                if i < k + 1:
+                    continue
+                t = i - (k + 1)
+                ps[i] = tk * np.dot(rows[i][k + 1:], v)
+                kp[r] += ps[i] * v[t]
+        half = 0.5 * tk * sum(kp)
+        wv = np.array([ps[k + 1 + t] - half * v[t] for t in range(m1)])
+        nrm = [0.0] * csize
+        for r in range(csize):
+            for i in own[r]:
+                if i < k + 1:
+                    continue
+                t = i - (k + 1)
+                rows[i][k + 1:] -= v[t] * wv + wv[t] * v
+                if t >= 2:
+                    nrm[r] += rows[i][k + 1] ** 2
+    d[n - 2], d[n - 1], e[n - 2] = rows[n - 2][n - 2], rows[n - 1][n - 1], rows[n - 1][n - 2]
+    return d, e, tau, refl
+
+
+@pytest.mark.parametrize("n", [13, 40, 67])
+def test_onchip_cluster_model_against_lapack(n):
+    """The model's tridiagonal has the eigenvalues of A, and the reflectors
+    (v_k with v_0 = 1 in row k, tau_k) rebuild A = Q T Q^T."""
+    rng = np.random.default_rng(n)
+    a = rng.normal(size=(n, n))
+    a = a + a.T
+    a[:5, 5:] = 0.0  # two decoupled blocks: column 4 is zero below the
+    a[5:, :5] = 0.0  # diagonal at step 4 (the tau = 0 branch)
+    d, e, tau, refl = onchip_cluster_tridiag(a)
+    assert tau[4] == 0.0
+    t = np.diag(d) + np.diag(e[:-1], 1) + np.diag(e[:-1], -1)
+    assert np.allclose(np.linalg.eigvalsh(t), np.linalg.eigvalsh(a), atol=1e-10)
+    q = np.eye(n)
+    for k in range(n - 2):
+        v = np.zeros(n)
+        v[k + 1:] = refl[k, k + 1:]
+        q = q @ (np.eye(n) - tau[k] * np.outer(v, v))
+    assert np.allclose(q @ t @ q.T, a, atol=1e-10)
