@@ -492,7 +492,7 @@ __global__ void __launch_bounds__(kMixThreads) k_charges_mix(DevParams p, DevPla
     if (flag == 3) {
       w.status[m] |= GBXTB_MOL_NONFINITE;
       w.phase[m] = kPhaseDone;
-    } else if (flag) {
+    } else if (flag == 1 || flag == 2) {
       if (flag == 2) w.status[m] |= GBXTB_MOL_NOT_CONVERGED;
       w.phase[m] = kPhaseFinal;
     }
