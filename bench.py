@@ -51,7 +51,16 @@ PORT_VS_REFERENCE = ("numpy restatement 9.1 s (energy + forces) vs dxtb 14.5 s (
                      "than the reference itself")
 
 
-def workload_config(world: int, nmol: int = NMOL) -> dict:
+def workload_config(world: int, nmol: int = NMOL, workload: str = "batch") -> dict:
+    if workload == "forces":
+        return {
+            "workload": f"{nmol} synthetic CHNO molecules per GPU, 30-60 atoms (uniform), positions perturbed by "
+                        "N(0, 0.05 bohr), energy + forces, SCF |dv|<1e-10, Fermi 300 K, D3 excluded",
+            "molecules_per_gpu": nmol, "global_batch": nmol * world, "atoms": "30-60",
+            "basis_functions": "90-180",
+            "parallelism": f"molecule shards x{world}" if world > 1 else "single GPU",
+            "l2": "inputs larger than L2 (workspace > 200 MB per call, rewritten every step)",
+        }
     return {
         "workload": f"{nmol} synthetic CHNO molecules per GPU, 10-120 atoms (uniform), energy + forces, "
                     "SCF |dv|<1e-10, Fermi 300 K, D3 excluded",
@@ -265,6 +274,65 @@ def run_reference_arm(args, rank: int, world: int) -> None:
     print(json.dumps(out), flush=True)
 
 
+def run_single(args, rank: int, world: int, local: int) -> None:
+    """The plain single point: one neutral 20-atom molecule, energy and
+    forces through the calculator's autograd path (get_energy on positions
+    that require grad, then torch.autograd.grad), one molecule per call.
+    Beside it the same single point on the host cores (numpy restatement,
+    one thread, as the reference runs one molecule)."""
+    import torch
+
+    from dxtb_gb300 import GFN1Calculator, molgen
+
+    num, pos = molgen.c1_single()[0]
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        import multiprocessing as mp
+
+        ctx = mp.get_context("spawn")
+        with ctx.Pool(1, initializer=_limit_threads) as pool:
+            pool.map(_cpu_one, [(num, pos)])
+            t = time.perf_counter()
+            reps = 10
+            pool.map(_cpu_one, [(num, pos)] * reps)
+            dt = time.perf_counter() - t
+        cpu = {"value": reps / dt, "unit": "single points/s", "cores": 1, "kind": "port",
+               "sample": f"the same 20-atom molecule, {reps} single points with forces, numpy restatement "
+                         "of the reference path incl. its Anderson mixer, one thread",
+               "vs_reference_itself": PORT_VS_REFERENCE}
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    calc = GFN1Calculator(torch.as_tensor(num), opts=OPTS)
+    host = torch.tensor(pos).pin_memory()
+
+    def one(p_host):
+        p = p_host.to(dev, non_blocking=True).requires_grad_(True)
+        e = calc.get_energy(p)
+        (g,) = torch.autograd.grad(e, p)
+        return e.item(), g.cpu()
+
+    for _ in range(args.warmup):
+        one(host)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        one(host)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    out = {"metric": METRIC, "value": args.steps / dt, "unit": "single points/s", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded CHNO molecule)",
+           "config": {"workload": "one neutral 20-atom molecule, energy + forces via autograd, SCF |dv|<1e-10, "
+                                  "Fermi 300 K, D3 excluded, one call per single point (host positions in, "
+                                  "energy and gradient out)"},
+           "e2e": {"value": args.steps / dt, "unit": "single points/s", "h2d_bytes_per_step": int(pos.size * 8),
+                   "d2h_bytes_per_step": int(8 + pos.size * 8)},
+           "cpu_baseline": cpu}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
 def run_large(args, rank: int, world: int, local: int) -> None:
     """Large molecules: the first K of 16 molecules of
     1000-2000 atoms (3000-6000 AOs), energies and forces in one call."""
@@ -392,6 +460,9 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain per-molecule GPU leg")
     ap.add_argument("--nmol", type=int, default=NMOL, help="molecules per GPU (profiling of smaller cases)")
+    ap.add_argument("--workload", default="batch", choices=["batch", "forces", "single"],
+                    help="batch: 512 x 10-120 atoms (the headline); forces: 256 x 30-60 atoms, perturbed; "
+                         "single: one 20-atom molecule per call")
     ap.add_argument("--fp64-only", action="store_true", help="disable the FP32 SCF passes")
     ap.add_argument("--no-replay", action="store_true",
                     help="skip the extra call with the reference's mixer (parity_reference_mixer)")
@@ -420,11 +491,26 @@ def main() -> None:
     if args.large or args.large_atoms:
         run_large(args, rank, world, local)
         return
+    if args.workload == "single":
+        run_single(args, rank, world, local)
+        return
 
     from dxtb_gb300 import replicas
 
-    nmol = args.nmol
-    mols = replicas.batch_shard(rank, NMOL)[:nmol]
+    from dxtb_gb300 import molgen
+
+    if args.workload == "forces":
+        # the 256-molecule force workload (30-60 atoms, perturbed positions);
+        # every rank runs the same molecules
+        nmol = min(args.nmol, 256)
+        mols = molgen.c3_forces(256)[:nmol]
+        full = 256
+        ref_name = "workload_forces_ref.npz"
+    else:
+        nmol = args.nmol
+        mols = replicas.batch_shard(rank, NMOL)[:nmol]
+        full = NMOL
+        ref_name = "workload_batch_ref.npz"
 
     # host-core baseline first (spawned workers, before any CUDA call)
     cpu = None
@@ -432,7 +518,7 @@ def main() -> None:
         procs = os.cpu_count() or 1
         v, dt = cpu_throughput(mols[:CPU_SAMPLE], procs)
         cpu = {"value": v, "unit": UNIT, "cores": procs, "kind": "port",
-               "sample": f"first {CPU_SAMPLE} of the 512 molecules, energy + forces, numpy restatement of "
+               "sample": f"first {CPU_SAMPLE} of the {full} molecules, energy + forces, numpy restatement of "
                          f"the reference path incl. its Anderson mixer, one process per core ({dt:.1f} s)",
                "vs_reference_itself": PORT_VS_REFERENCE}
 
@@ -533,8 +619,8 @@ def main() -> None:
     # and of one call that replays the reference's own SCF (its Anderson
     # mixer, every pass in FP64), outside the timed region
     parity = replay = None
-    ref_path = ROOT / "tests" / "golden" / "workload_batch_ref.npz"
-    if rank == 0 and ref_path.exists() and nmol == NMOL:
+    ref_path = ROOT / "tests" / "golden" / ref_name
+    if rank == 0 and ref_path.exists() and nmol == full:
         ref = np.load(ref_path)
         parity = parity_summary(res, ref, t_dev / args.steps)
         if not args.no_replay:
@@ -549,7 +635,7 @@ def main() -> None:
             torch.cuda.synchronize()
             t_r = er0.elapsed_time(er1) / 1e3
             replay = {"mode": "mixer=anderson (the reference's), every SCF pass in FP64", "seconds": t_r,
-                      "rate": NMOL / t_r, **parity_summary(rr, ref, t_r)}
+                      "rate": nmol / t_r, **parity_summary(rr, ref, t_r)}
 
     # roofline of the dominant kernel class: FP64-pipe-equivalent rate
     # (an FP32 FMA counts 1/64 of an FP64 FMA, the ratio of the two pipes)
@@ -579,7 +665,7 @@ def main() -> None:
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded CHNO molecules)", "config": workload_config(world, nmol),
+            "data": "synthetic (seeded CHNO molecules)", "config": workload_config(world, nmol, args.workload),
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(nbytes_in),
                     "d2h_bytes_per_step": int(nbytes_out)},
             "gpu_launches": int(launches),
