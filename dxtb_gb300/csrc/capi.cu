@@ -600,8 +600,10 @@ int gbxtb_singlepoint(gbxtb_plan *plan, const gbxtb_options *opts, const double 
   Prof pf{plan, s, opts->profile != 0};
   rc = enqueue_setup(plan, w, *opts, positions_dev, s, pf);
   if (rc) return rc;
-  // SCF: maxiter mixing iterations + the first evaluation + the final pass
-  const int max_loops = opts->maxiter + 3;
+  // SCF: maxiter mixing iterations + the first evaluation + the final pass,
+  // and with restart_at the passes before the restart on top (a restarted
+  // molecule gets a fresh maxiter budget)
+  const int max_loops = opts->maxiter + 3 + (opts->restart_at > 0 ? opts->restart_at : 0);
   int active = pl.nmol;  // molecules iterating (known after each pass)
   int nclus = 0;         // of those, passes that tridiagonalise on a cluster
   launch_count_active(pl, w, s);
@@ -670,6 +672,11 @@ int gbxtb_singlepoint(gbxtb_plan *plan, const gbxtb_options *opts, const double 
     nclus = plan->h_active[1];
     if (active == 0) break;
   }
+  // every molecule ends within max_loops passes; one still iterating would
+  // have no final state, so it is an error, never a silent result
+  if (active != 0)
+    return fail(GBXTB_ERR_CUDA, "internal: " + std::to_string(active) + " molecules still iterating after " +
+                                    std::to_string(max_loops) + " SCF passes");
   launch_energies(p, pl, w, opts->kt, energy_dev, charges_dev, s);
   plan->total_launches += 1;
   if (opts->want_forces) {
