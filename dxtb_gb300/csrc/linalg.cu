@@ -886,9 +886,15 @@ template <typename T>
 __host__ __device__ constexpr size_t onchip_smem_bytes(int n) {
   return sizeof(T) * ((size_t)((n + kClusterSize - 1) / kClusterSize) * (n + 1) + 2 * (size_t)n);
 }
+// Molecules whose rows need at most this much shared memory per CTA run in
+// a launch sized for it, which lets two CTAs share an SM (FP64 up to 320
+// AOs, every FP32 pass up to 400); the others in a launch with one CTA per
+// SM.  The SCF's tridiagonalisation is latency-bound, so two clusters per
+// set of SMs keep the pipes busier.
+constexpr size_t kOnchipSmallBytes = 110 * 1024;
 
 __global__ void __cluster_dims__(kClusterSize, 1, 1) __launch_bounds__(kTrdClThreads)
-    k_tridiag_cluster(DevPlan pl, Work w, const int32_t *mol_list, int tail) {
+    k_tridiag_cluster(DevPlan pl, Work w, const int32_t *mol_list, int tail, int big) {
   cg::cluster_group cluster = cg::this_cluster();
   const int m = list_mol(w, mol_list, blockIdx.x / kClusterSize);
   if (m < 0) return;  // the whole cluster
@@ -901,7 +907,10 @@ __global__ void __cluster_dims__(kClusterSize, 1, 1) __launch_bounds__(kTrdClThr
   // kTailClusterMinN AOs), molecules above kClusterBlockedMinN AOs in
   // k_tridiag_cluster_blocked
   const bool smem32 = w.prec[m] == 0 && md.nao <= kSmemTridiagMaxN && !(tail && md.nao > kTailClusterMinN);
-  const bool done = (w.phase[m] == kPhaseDone) || smem32 || md.nao > kClusterBlockedMinN;
+  // the launch for small or for large shared-memory needs
+  const size_t need = w.prec[m] ? onchip_smem_bytes<double>(md.nao) : onchip_smem_bytes<float>(md.nao);
+  const bool other_launch = big ? need <= kOnchipSmallBytes : need > kOnchipSmallBytes;
+  const bool done = (w.phase[m] == kPhaseDone) || smem32 || md.nao > kClusterBlockedMinN || other_launch;
   if (!done) {
     if (w.prec[m])
       tridiag_cluster_onchip<double>(cluster, md, w, sm, red, nrm2, kp2);
@@ -1926,12 +1935,19 @@ void launch_tridiag_smem(const DevPlan &pl, const Work &w, cudaStream_t s, bool 
 int launch_tridiag_cluster(const DevPlan &pl, const Work &w, const int32_t *mol_list, int count, int maxn,
                            cudaStream_t s, bool tail) {
   if (count <= 0) return 0;
-  const size_t smem = onchip_smem_bytes<double>(min(maxn, kClusterBlockedMinN));
-  k_tridiag_cluster<<<count * kClusterSize, kTrdClThreads, smem, s>>>(pl, w, mol_list, tail ? 1 : 0);
-  if (maxn <= kClusterBlockedMinN) return 1;
+  // two size classes of shared memory (kOnchipSmallBytes)
+  const size_t need = onchip_smem_bytes<double>(min(maxn, kClusterBlockedMinN));
+  const size_t small = need < kOnchipSmallBytes ? need : kOnchipSmallBytes;
+  k_tridiag_cluster<<<count * kClusterSize, kTrdClThreads, small, s>>>(pl, w, mol_list, tail ? 1 : 0, 0);
+  int launches = 1;
+  if (need > kOnchipSmallBytes) {
+    k_tridiag_cluster<<<count * kClusterSize, kTrdClThreads, need, s>>>(pl, w, mol_list, tail ? 1 : 0, 1);
+    ++launches;
+  }
+  if (maxn <= kClusterBlockedMinN) return launches;
   k_tridiag_cluster_blocked<<<count * kClusterSize, kTrdBlkThreads, tridiag_cluster_smem_bytes(maxn), s>>>(
       pl, w, mol_list);
-  return 2;
+  return launches + 1;
 }
 
 // All molecules (mol_list null, count = nmol) with 256 threads per block,
