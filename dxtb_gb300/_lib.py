@@ -28,7 +28,7 @@ EXPORTED = (
     "gbxtb_fp64_peak", "gbxtb_get_fp32_passes", "gbxtb_singlepoint_noalloc",
     "gbxtb_pool_create", "gbxtb_pool_destroy", "gbxtb_pool_free_slots", "gbxtb_pool_admit",
     "gbxtb_pool_step_launch", "gbxtb_pool_step_finish", "gbxtb_pool_result", "gbxtb_pool_step_poll",
-    "gbxtb_plan_autotune", "gbxtb_default_options", "gbxtb_forces",
+    "gbxtb_plan_autotune", "gbxtb_default_options", "gbxtb_forces", "gbxtb_pool_evict",
 )
 
 NOALLOC_SCRATCH_BYTES = 32 * 1024 * 1024  # GBXTB_NOALLOC_SCRATCH_BYTES
@@ -142,6 +142,8 @@ def load() -> C.CDLL:
     lib.gbxtb_pool_admit.argtypes = [vp, C.c_int32, i32p, f64p, C.c_double, C.c_int32, i32p]
     lib.gbxtb_pool_step_launch.argtypes = [vp, vp]
     lib.gbxtb_pool_step_poll.argtypes = [vp]
+    lib.gbxtb_pool_evict.argtypes = [vp, C.c_int32, vp]
+    lib.gbxtb_pool_evict.restype = C.c_int
     lib.gbxtb_plan_autotune.argtypes = [vp, C.POINTER(Options), vp, vp, C.c_size_t, vp, C.POINTER(C.c_int32)]
     lib.gbxtb_pool_step_finish.argtypes = [vp, i32p, i32p, i32p]
     lib.gbxtb_pool_result.argtypes = [vp, C.c_int32, f64p, f64p, f64p, i32p, i32p]

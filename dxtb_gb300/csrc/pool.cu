@@ -75,6 +75,15 @@ __global__ void k_pool_begin(DevPlan pl, Work w, const int32_t *slots, int n) {
   w.active[1] = big;
 }
 
+// Evict one iterating slot between steps: it no longer takes part in the
+// passes, is not reported as ended, and the device lists of iterating
+// molecules are rebuilt without it (k_count_active runs after this).
+__global__ void k_pool_evict(Work w, int32_t *inflight, int slot) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  w.phase[slot] = kPhaseDone;
+  inflight[slot] = 0;
+}
+
 // Slots that ended in this step (converged, hit maxiter, or failed): list
 // them for the host and free their phase.  out[0] = count, out[1..] slots;
 // out[nslots + 1], out[nslots + 2] = iterating molecules, large FP64 passes.
@@ -506,6 +515,20 @@ int gbxtb_pool_step_finish(gbxtb_pool *pool, int32_t *ended, int32_t *nended, in
   pool->active = o[pool->nslots + 1];
   pool->nclus = o[pool->nslots + 2];
   if (iterating) *iterating = pool->active;
+  return GBXTB_OK;
+}
+
+int gbxtb_pool_evict(gbxtb_pool *pool, int32_t slot, void *stream) {
+  if (!pool || slot < 0 || slot >= pool->nslots) return fail(GBXTB_ERR_ARG, "bad slot");
+  if (pool->launched) return fail(GBXTB_ERR_ARG, "a step is in flight; finish it first");
+  if (pool->state[slot] != 2) return fail(GBXTB_ERR_ARG, "slot holds no iterating molecule");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  k_pool_evict<<<1, 32, 0, s>>>(pool->w, pool->inflight, slot);
+  launch_count_active(pool->plan->pl, pool->w, s);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(s));
+  pool->state[slot] = 0;
+  pool->free_slots.push_back(slot);
   return GBXTB_OK;
 }
 

@@ -11,7 +11,16 @@ take the next requests, so requests that arrive while others are on the GPU
 join the running batch instead of waiting for it to drain.
 
 Slot counts follow a device-memory budget: a slot of capacity N AOs holds
-its molecule's SCF state (about 14 N^2 doubles).
+its molecule's SCF state (about 14 N^2 doubles).  A molecule goes to the
+smallest class whose atom, shell and orbital capacity it fits; one that fits
+no class is refused at submission.
+
+Stragglers: with ``evict_after`` set, a molecule still iterating after that
+many passes leaves its slot (``gbxtb_pool_evict``) and is solved again from
+the start in a small pool of the same class reserved for such molecules.
+A fresh SCF of the same molecule takes the same path, so its result is the
+one it would have had; the main slots stop being held for up to ``maxiter``
+passes by molecules that converge slowly or not at all.
 
 Per molecule the result is the single point of
 ``dxtb_gb300.GFN1Calculator`` (the reference's ``get_energy`` /
@@ -31,7 +40,7 @@ import torch
 from . import _lib, params
 from .calculator import _Context, engine_options, resolve_opts
 
-__all__ = ["Server", "Request", "size_class_capacity"]
+__all__ = ["Server", "Request", "size_class_capacity", "molecule_size"]
 
 # (max atoms, share of the memory budget) of the default size classes
 DEFAULT_CLASSES = ((32, 0.15), (100, 0.25), (200, 0.3), (400, 0.3))
@@ -43,6 +52,19 @@ def size_class_capacity(max_atoms: int) -> tuple[int, int]:
     main-group elements without d shells: two shells, at most four AOs per
     atom); larger molecules go to a larger class."""
     return 2 * max_atoms, 4 * max_atoms
+
+
+def molecule_size(numbers) -> tuple[int, int]:
+    """(shells, AOs) of a molecule."""
+    elems = params.raw()["elements"]
+    nsh = nao = 0
+    for z in np.asarray(numbers).tolist():
+        el = elems.get(str(int(z)))
+        if el is None:
+            raise ValueError(f"atomic number {z} has no GFN1 parameters")
+        nsh += len(el["shells"])
+        nao += sum(2 * s["l"] + 1 for s in el["shells"])
+    return nsh, nao
 
 
 def slot_bytes(max_atoms: int) -> int:
@@ -68,6 +90,8 @@ class Request:
     status: int | None = None
     iterations: int | None = None
     size_class: int | None = None
+    passes: int = 0        # SCF passes run in its current slot
+    evicted: bool = False  # moved to a straggler pool
 
     @property
     def latency(self) -> float | None:
@@ -83,6 +107,7 @@ class _Pool:
         self.max_atoms = max_atoms
         self.nslots = nslots
         nsh, nao = size_class_capacity(max_atoms)
+        self.cap_sh, self.cap_ao = nsh, nao
         h = C.c_void_p()
         nbytes = C.c_size_t()
         with torch.cuda.device(device):
@@ -100,6 +125,15 @@ class _Pool:
 
     def free(self) -> int:
         return int(self.lib.gbxtb_pool_free_slots(self.handle))
+
+    def fits(self, req: Request) -> bool:
+        nsh, nao = molecule_size(req.numbers)
+        return len(req.numbers) <= self.max_atoms and nsh <= self.cap_sh and nao <= self.cap_ao
+
+    def evict(self, slot: int) -> Request:
+        """Take the molecule of `slot` out (between steps) and return its request."""
+        _lib.check(self.lib.gbxtb_pool_evict(self.handle, int(slot), C.c_void_p(self.stream.cuda_stream)))
+        return self.requests.pop(slot)
 
     def admit(self, req: Request) -> bool:
         num = np.ascontiguousarray(req.numbers, dtype=np.int32)
@@ -168,7 +202,8 @@ class Server:
     ``opts``: calculator options (``dxtb_gb300.calculator.DEFAULT_OPTS``)."""
 
     def __init__(self, classes=DEFAULT_CLASSES, opts: dict | None = None, memory_gb: float = 16.0,
-                 device: int | None = None, max_slots: int = 512):
+                 device: int | None = None, max_slots: int = 512, evict_after: int | None = None,
+                 straggler_share: float = 0.15):
         if device is None:
             device = torch.cuda.current_device()
         self.device = device
@@ -178,7 +213,9 @@ class Server:
         opt = engine_options(o, forces=True)
         self.opts = o
         ctx = _Context.get(device)
+        self.evict_after = evict_after
         self.pools: list[_Pool] = []
+        self.slow: list[_Pool] = []  # straggler pools, one per class (with evict_after)
         for rank, (max_atoms, amount) in enumerate(sorted(classes)):
             amount = float(amount)
             if amount < 1:
@@ -186,23 +223,31 @@ class Server:
             else:
                 nslots = int(amount)
             nslots = max(1, min(max_slots, nslots))
+            nslow = max(1, int(round(straggler_share * nslots))) if evict_after else 0
             # priority -1 (high) for the two smallest classes, 0 (normal) for the rest
-            self.pools.append(_Pool(ctx, opt, int(max_atoms), nslots, device, priority=-1 if rank <= 1 else 0))
+            prio = -1 if rank <= 1 else 0
+            self.pools.append(_Pool(ctx, opt, int(max_atoms), max(1, nslots - nslow), device, priority=prio))
+            if nslow:
+                self.slow.append(_Pool(ctx, opt, int(max_atoms), nslow, device, priority=prio))
         self.queue: deque[Request] = deque()
+        self.slow_queue: deque[Request] = deque()
         self.completed: list[Request] = []
         self._next_id = 0
         self.steps = 0
 
     @property
     def device_bytes(self) -> int:
-        return sum(p.device_bytes for p in self.pools)
+        return sum(p.device_bytes for p in self.pools + self.slow)
 
     def submit(self, numbers, positions, charge: float = 0.0, spin: int | None = None,
                t_submit: float | None = None) -> Request:
         """Queue one single point (host arrays; positions in bohr)."""
         num = np.asarray(numbers)
-        if len(num) > self.pools[-1].max_atoms:
-            raise ValueError(f"molecule with {len(num)} atoms exceeds the largest size class")
+        nsh, nao = molecule_size(num)
+        big = self.pools[-1]
+        if len(num) > big.max_atoms or nsh > big.cap_sh or nao > big.cap_ao:
+            raise ValueError(f"molecule with {len(num)} atoms, {nsh} shells and {nao} orbitals exceeds the "
+                             f"largest size class ({big.max_atoms} atoms, {big.cap_sh} shells, {big.cap_ao} orbitals)")
         req = Request(self._next_id, num, np.asarray(positions, dtype=np.float64), float(charge), spin,
                       time.perf_counter() if t_submit is None else t_submit)
         self._next_id += 1
@@ -219,19 +264,31 @@ class Server:
         return self.submit(mol["numbers"], mol["positions"], mol["charge"], mol["uhf"], t_submit)
 
     def _admit(self) -> None:
-        waiting = deque()
-        while self.queue:
-            req = self.queue.popleft()
-            placed = False
-            for c, pool in enumerate(self.pools):
-                if len(req.numbers) <= pool.max_atoms and pool.free() > 0 and pool.admit(req):
-                    req.t_admit = time.perf_counter()
-                    req.size_class = c
-                    placed = True
-                    break
-            if not placed:
-                waiting.append(req)
-        self.queue = waiting
+        for queue, pools in ((self.queue, self.pools), (self.slow_queue, self.slow)):
+            waiting = deque()
+            while queue:
+                req = queue.popleft()
+                placed = False
+                for c, pool in enumerate(pools):
+                    if pool.fits(req) and pool.free() > 0 and pool.admit(req):
+                        if req.t_admit is None:
+                            req.t_admit = time.perf_counter()
+                        req.size_class = c
+                        req.passes = 0
+                        placed = True
+                        break
+                if not placed:
+                    waiting.append(req)
+            queue.extend(waiting)
+
+    def _evict_stragglers(self, pool: "_Pool") -> None:
+        """After a finished step of a main pool: molecules that have run
+        evict_after passes there move to the straggler pools."""
+        for slot, req in list(pool.requests.items()):
+            req.passes += 1
+            if self.evict_after and req.passes >= self.evict_after:
+                self.slow_queue.append(pool.evict(slot))
+                req.evicted = True
 
     def step(self, wait: bool = True) -> list[Request]:
         """Advance every pool at its own pace: collect the pools whose step
@@ -243,15 +300,17 @@ class Server:
         when every busy pool is still running."""
         done = []
         while True:
-            for p in self.pools:
+            for p in self.pools + self.slow:
                 if p.launched and p.ready():
                     done.extend(p.finish())
+                    if self.evict_after and p in self.pools:
+                        self._evict_stragglers(p)
             self._admit()
-            for p in self.pools:
+            for p in self.pools + self.slow:
                 if not p.launched and p.busy:
                     p.launch()
                     self.steps += 1
-            if done or not wait or not any(p.launched for p in self.pools):
+            if done or not wait or not any(p.launched for p in self.pools + self.slow):
                 break
             time.sleep(5e-5)
         now = time.perf_counter()
@@ -262,7 +321,8 @@ class Server:
 
     @property
     def idle(self) -> bool:
-        return not self.queue and not any(p.busy or p.launched for p in self.pools)
+        return (not self.queue and not self.slow_queue
+                and not any(p.busy or p.launched for p in self.pools + self.slow))
 
     def run_until_idle(self, max_steps: int = 100000) -> list[Request]:
         out = []

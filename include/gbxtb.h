@@ -310,6 +310,15 @@ GBXTB_API int gbxtb_pool_step_poll(gbxtb_pool *pool);
 GBXTB_API int gbxtb_pool_step_finish(gbxtb_pool *pool, int32_t *ended, int32_t *nended,
                                      int32_t *iterating);
 
+/* Take an iterating molecule out of the pool between steps (no step in
+ * flight) and free its slot; it is not reported as ended.  A server uses it
+ * to move a molecule that has not converged after many passes out of the
+ * way of new requests and to solve it again elsewhere (a fresh SCF of the
+ * same molecule gives the same result, so nothing is lost but the passes
+ * already spent).  No counterpart in the reference (it has no serving
+ * form). */
+GBXTB_API int gbxtb_pool_evict(gbxtb_pool *pool, int32_t slot, void *stream);
+
 /* Result of an ended slot (host arrays: energy[1], charges[natoms],
  * gradient[natoms][3] = dE/dR, status[1], iterations[1]; each nullable);
  * frees the slot. */

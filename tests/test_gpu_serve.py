@@ -84,3 +84,24 @@ def test_oversized_request_is_refused():
     num, pos = molgen.grow(30, 7)
     with pytest.raises(ValueError):
         srv.submit(num, pos)
+
+
+def test_stragglers_leave_their_slots_and_keep_their_results():
+    """evict_after = 12 passes: molecules still iterating then move to the
+    straggler pool of their class and are solved again there; every result
+    still equals the solo single point, and the evicted molecules are the
+    ones whose solo SCF needs more passes."""
+    from dxtb_gb300.serve import Server
+
+    mols = molgen.workload(3, 10, 8, 60, log_uniform=True)
+    srv = Server(classes=((24, 3), (60, 3)), opts=TIGHT, evict_after=12, straggler_share=0.34)
+    for num, pos in mols:
+        srv.submit(num, pos)
+    srv.run_until_idle()
+    reqs = sorted(srv.completed, key=lambda r: r.id)
+    assert len(reqs) == len(mols) and srv.idle
+    assert any(r.evicted for r in reqs)
+    assert check_against_solo(reqs) >= len(mols) - 1
+    for r in reqs:
+        if r.evicted and r.status == 0:
+            assert r.iterations + 1 >= 12

@@ -73,10 +73,17 @@ class _FakePool:
 
     def __init__(self, max_atoms, nslots, passes=2):
         self.max_atoms, self.nslots, self.passes = max_atoms, nslots, passes
+        self.cap_sh, self.cap_ao = serve.size_class_capacity(max_atoms)
         self.requests = {}
         self.left = {}
         self.launched = False
         self.iterating = 0
+
+    fits = serve._Pool.fits
+
+    def evict(self, slot):
+        self.left.pop(slot)
+        return self.requests.pop(slot)
 
     def free(self):
         return self.nslots - len(self.requests)
@@ -112,10 +119,13 @@ class _FakePool:
         return bool(self.requests)
 
 
-def _server_with_fake_pools(classes):
+def _server_with_fake_pools(classes, evict_after=None, slow=(), passes=2):
     srv = serve.Server.__new__(serve.Server)
-    srv.pools = [_FakePool(a, n) for a, n in classes]
+    srv.pools = [_FakePool(a, n, passes) for a, n in classes]
+    srv.slow = [_FakePool(a, n, passes) for a, n in slow]
+    srv.evict_after = evict_after
     srv.queue = serve.deque()
+    srv.slow_queue = serve.deque()
     srv.completed = []
     srv._next_id = 0
     srv.steps = 0
@@ -150,3 +160,30 @@ def test_oversized_request_is_refused_on_the_host():
     srv = _server_with_fake_pools([(10, 1)])
     with pytest.raises(ValueError):
         srv.submit(np.ones(11, dtype=np.int64), np.zeros((11, 3)))
+
+
+def test_request_that_fits_no_class_by_orbitals_is_refused():
+    """A molecule within the atom capacity whose d-shell elements need more
+    orbitals than the largest class holds is refused, not left waiting."""
+    import pytest
+
+    srv = _server_with_fake_pools([(10, 1)])
+    srv.submit(np.array([6] * 10), np.zeros((10, 3)))  # 40 AOs: fits
+    with pytest.raises(ValueError, match="orbitals"):
+        srv.submit(np.array([35] * 10), np.zeros((10, 3)))  # Br: s, p, d shells
+
+
+def test_stragglers_move_to_the_straggler_pool():
+    """With evict_after = 3 passes and molecules needing 5, every molecule
+    leaves its main slot after 3 passes, restarts in the straggler pool and
+    finishes there; the main slot takes the next request meanwhile."""
+    srv = _server_with_fake_pools([(40, 1)], evict_after=3, slow=[(40, 1)], passes=5)
+    for n in (5, 6):
+        srv.submit(np.ones(n, dtype=np.int64), np.zeros((n, 3)))
+    srv.run_until_idle()
+    assert srv.idle
+    assert sorted(r.id for r in srv.completed) == [0, 1]
+    assert all(r.evicted and r.status == 0 for r in srv.completed)
+    # request 1 entered the main slot while request 0 finished in the straggler pool
+    by_id = {r.id: r for r in srv.completed}
+    assert by_id[1].t_admit < by_id[0].t_done
