@@ -392,7 +392,8 @@ def run_serve(args, rank: int, world: int, local: int) -> None:
     warnings.simplefilter("ignore")
     nreq = args.serve_requests
     mols = molgen.c4_stream(nreq)
-    srv = Server(opts=OPTS, memory_gb=24.0)
+    evict = args.serve_evict if args.serve_evict > 0 else None
+    srv = Server(opts=OPTS, memory_gb=24.0, evict_after=evict)
     # warm-up: a few molecules of every size class
     for num, pos in sorted(mols, key=lambda m: len(m[0]))[:: max(1, nreq // 8)]:
         srv.submit(num, pos)
@@ -419,10 +420,11 @@ def run_serve(args, rank: int, world: int, local: int) -> None:
             t_end = max(r.t_done for r in srv.completed)
             lat = latency_summary(srv.completed)
             conv = sum(1 for r in srv.completed if r.status == 0)
+            ev = sum(1 for r in srv.completed if r.evicted)
             sweep.append({"rate_req_s": rate, "throughput": nreq / (t_end - t0), **lat, "converged": conv,
-                          "steps": srv.steps})
-    # plain one-at-a-time path over the same molecules (a sample)
-    sample = mols[: min(24, nreq)]
+                          "evicted_stragglers": ev, "steps": srv.steps})
+    # plain one-at-a-time path over the same molecules (a size-matched sample)
+    sample = [mols[i] for i in size_matched(mols, min(24, nreq))]
     calcs = [GFN1Calculator(torch.as_tensor(a), opts=OPTS) for a, _ in sample]
     for c, (_, b) in zip(calcs, sample):
         c.singlepoint(torch.tensor(b, device="cuda"), forces=True)
@@ -441,9 +443,13 @@ def run_serve(args, rank: int, world: int, local: int) -> None:
                                "log-uniform, energy + forces, SCF |dv|<1e-10, continuous batching over "
                                f"{len(srv.pools)} size-class slot pools",
                    "pools": [{"max_atoms": p.max_atoms, "slots": p.nslots} for p in srv.pools],
+                   "straggler_pools": [{"max_atoms": p.max_atoms, "slots": p.nslots} for p in srv.slow],
+                   "evict_after_passes": evict,
                    "device_bytes": srv.device_bytes},
         "served": sweep,
-        "plain_per_molecule": {"value": plain, "unit": UNIT, "sample": f"first {len(sample)} requests, one call each"},
+        "plain_per_molecule": {"value": plain, "unit": UNIT,
+                               "sample": f"{len(sample)} of the requests at evenly spaced quantiles of the atom "
+                                         "count, one engine call each"},
         "served_over_plain": best["throughput"] / plain,
         "clocks": clk.summary(),
     }
@@ -470,6 +476,8 @@ def main() -> None:
                     help="served stream instead of the batch: Poisson arrivals, 8-400 atoms, continuous batching")
     ap.add_argument("--serve-requests", type=int, default=96, help="requests per arrival rate")
     ap.add_argument("--serve-rates", default="100,200,500,1000,2000,5000", help="arrival rates (req/s)")
+    ap.add_argument("--serve-evict", type=int, default=60,
+                    help="passes after which a served molecule moves to a straggler pool (0: never)")
     ap.add_argument("--large", type=int, default=0, metavar="K",
                     help="large molecules instead of the batch: K of the 16 molecules of 1000-2000 atoms")
     ap.add_argument("--large-atoms", default="", metavar="N1,N2",

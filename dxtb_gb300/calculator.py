@@ -57,7 +57,7 @@ DEFAULT_OPTS = {
     # reference's Anderson mixer step for step (what its default full-mode SCF
     # runs, scf/unrolling/base.py:81-99); "simple": linear mixing
     "mixer": "broyden",
-    "broyden_alpha": 0.3,
+    "broyden_alpha": 0.2,    # fastest of 0.1-0.5 on the 512-molecule workload, and the closest to the reference
     "broyden_memory": 20,
     # Broyden/simple: a molecule still iterating after this many passes is
     # solved again from the guess with the reference's Anderson mixer (FP64),

@@ -139,7 +139,7 @@ void gbxtb_default_options(gbxtb_options *o) {
   o->x_atol = 1.0e-4;
   o->x_atol_max = 1.0e-5;
   o->kt = 300.0 * (1.3806488e-23 / 4.35974434e-18);  // 300 K in Hartree: k_B / E_h (CODATA 2010)
-  o->broyden_alpha = 0.3;
+  o->broyden_alpha = 0.2;
   o->profile = 0;
   o->mixed_precision = 0;
   o->mixer = GBXTB_MIXER_ANDERSON;

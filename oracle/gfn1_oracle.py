@@ -634,7 +634,7 @@ class Broyden:
     by the GPU engine: step alpha, weights 1, w0 = 0.01, ``memory`` most
     recent difference pairs."""
 
-    def __init__(self, alpha=0.3, memory=20, w0=0.01):
+    def __init__(self, alpha=0.2, memory=20, w0=0.01):
         self.alpha, self.memory, self.w0 = alpha, memory, w0
         self.df: list = []
         self.u: list = []
@@ -663,7 +663,7 @@ class Broyden:
 def singlepoint(numbers, positions, chrg: float = 0.0, spin=None, forces: bool = True,
                 etemp: float = 300.0, maxiter: int = 300, x_atol: float = 1e-10,
                 x_atol_max: float = 1e-10, mixer: str = "anderson",
-                broyden_alpha: float = 0.3, broyden_memory: int = 20,
+                broyden_alpha: float = 0.2, broyden_memory: int = 20,
                 v_init: np.ndarray | None = None, fermi_thr: float | None = None) -> Result:
     """GFN1 single point without dispersion (calculators/types/energy.py:78-402).
 
