@@ -498,6 +498,7 @@ __global__ void __launch_bounds__(NW * 32) k_tridiag_smem(DevPlan pl, Work w, co
   if (w.phase[m] == kPhaseDone || w.prec[m] != 0) return;
   const MolDesc md = pl.mol[m];
   const int n = md.nao;
+  if (n > kSmemTridiagMaxN) return;          // on a cluster (k_tridiag_cluster_blocked)
   if (tail && n > kTailClusterMinN) return;  // on a cluster (k_tridiag_cluster)
   const int k0 = n > kSmemLocalMaxN ? n - kSmemLocalMaxN : 0;  // steps in global memory
   const int nl = n - k0;                                        // trailing size on chip

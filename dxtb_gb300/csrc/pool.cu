@@ -231,10 +231,13 @@ int gbxtb_pool_create(gbxtb_ctx *ctx, const gbxtb_options *opts, int32_t nslots,
   d.npair = (int64_t)nslots * cap_shells * (cap_shells + 1) / 2;
   d.pool = 1;
   plan->ntile = tile0[nslots];
-  // every slot in the shared-memory size class of its capacity
+  // every slot in the shared-memory size class of its capacity; a pool
+  // whose capacity exceeds the on-chip limit still lists every slot in the
+  // largest class, since its molecules of up to kSmemTridiagMaxN AOs run
+  // their FP32 passes there (larger ones on a cluster)
   std::vector<int32_t> bin_slots(nslots);
   for (int m = 0; m < nslots; ++m) bin_slots[m] = m;
-  int bin = -1;
+  int bin = kSmemBins - 1;
   for (int c = 0; c < kSmemBins; ++c)
     if (cap_aos <= kSmemBinN[c]) {
       bin = c;
@@ -275,11 +278,11 @@ int gbxtb_pool_create(gbxtb_ctx *ctx, const gbxtb_options *opts, int32_t nslots,
   for (int c = 0; c < kSmemBins; ++c) {
     d.bin_mols[c] = (const int32_t *)(b + o_bin);
     d.bin_count[c] = (c == bin) ? nslots : 0;
-    d.bin_maxn[c] = (c == bin) ? cap_aos : 0;
+    d.bin_maxn[c] = (c == bin) ? std::min(cap_aos, kSmemTridiagMaxN) : 0;
     d.bin_warps[c] = kSmemBinWarps[c];
   }
   d.bisect_threads = 256;
-  plan->smem_launches = (bin >= 0) ? 1 : 0;
+  plan->smem_launches = 1;
   pool->pos = (double *)(b + o_pos);
   pool->grad = (double *)(b + o_grad);
   pool->inflight = (int32_t *)(b + o_infl);

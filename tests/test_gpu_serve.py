@@ -105,3 +105,19 @@ def test_stragglers_leave_their_slots_and_keep_their_results():
     for r in reqs:
         if r.evicted and r.status == 0:
             assert r.iterations + 1 >= 12
+
+
+def test_small_molecules_in_a_large_class():
+    """Molecules far below a class's capacity (here a class of up to 150
+    atoms, 600 orbitals, above the on-chip limit of the FP32
+    tridiagonalisation) are served correctly, whether the pool's passes
+    take the shapes of a full batch or of its tail."""
+    from dxtb_gb300.serve import Server
+
+    mols = molgen.workload(3, 6, 10, 60, log_uniform=True)
+    srv = Server(classes=((150, 6),), opts=TIGHT)
+    for num, pos in mols:
+        srv.submit(num, pos)
+    srv.run_until_idle()
+    assert len(srv.completed) == len(mols)
+    assert check_against_solo(srv.completed) >= len(mols) - 1
