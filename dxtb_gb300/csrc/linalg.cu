@@ -733,25 +733,46 @@ __device__ __forceinline__ T ld_cg(const T *p) {
 // cluster keep their own rows (row i on CTA i mod 8, full length n) in
 // shared memory for the whole tridiagonalisation, so that the matrix-vector
 // product and the rank-2 update of a step touch only local shared memory.
-// A step needs two cluster barriers:
-//   (a) every CTA sums the eight partial norms of column k published before
-//       the previous barrier, reads alpha from the owner of row k+1 and
-//       builds the reflector from the owners' column entries (distributed
-//       shared memory); (b) p = tau A22 v for its own rows and the partial
-//       p.v are published;  -- barrier 1 --
-//   (c) every CTA sums the partials, gathers p from the owners and forms
-//       w = p - tau/2 (p.v) v for all rows; (d) A22 -= v w^T + w v^T on its
-//       own rows, with the partial norm of column k+1 accumulated on the
-//       fly and published.  -- barrier 2 --
-// Every CTA computes tau, beta and the scale from the same eight partials
-// in the same order, so every branch on them is uniform over the cluster.
-// Partial norms and p.v partials are double-buffered by the parity of k: a
-// buffer is rewritten only after a barrier that follows its last read.
+// A step needs two cluster barriers and two CTA barriers:
+//   (a) every warp sums the 64 per-warp partial norms of column k published
+//       before the previous barrier (8 CTAs x 8 warps), reads alpha from the
+//       owner of row k+1, and the CTA builds the reflector from the owners'
+//       column entries (distributed shared memory);  -- CTA barrier --
+//   (b) p = tau A22 v for its own rows and per-warp partials of p.v are
+//       published;  -- cluster barrier 1 --
+//   (c) every warp sums the 64 partials of p.v, the CTA gathers p from the
+//       owners and forms w = p - tau/2 (p.v) v for all rows;  -- CTA barrier --
+//   (d) A22 -= v w^T + w v^T on its own rows, with the per-warp partial norm
+//       of column k+1 accumulated on the fly and published.
+//       -- cluster barrier 2 --
+// Every warp of every CTA sums the same 64 partials in the same order (a
+// fixed lane assignment and butterfly), so tau, beta and the scale are
+// bitwise the same everywhere and every branch on them is uniform over the
+// cluster.  Partials are double-buffered by the parity of k: a buffer is
+// rewritten only after a barrier that follows its last read.
 // Output conventions as tridiag_body (reflector k in row k of A in global
 // memory, d, e, tau).
+constexpr int kClWarps = kTrdClThreads / 32;  // warps per CTA of the cluster kernels
+
+// Sum over the cluster of the per-warp partials part[buf][0..kClWarps)
+// published by every CTA; every lane of the calling warp gets the sum.
+template <typename T>
+__device__ __forceinline__ T cluster_partial_sum(cg::cluster_group &cluster, T (*part)[kClWarps], int buf) {
+  static_assert(kClusterSize * kClWarps == 64, "two partials per lane");
+  const int lane = threadIdx.x & 31;
+  T v = T(0);
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int idx = lane + 32 * h;
+    v += cluster.map_shared_rank(&part[buf][0], idx / kClWarps)[idx % kClWarps];
+  }
+  return warp_sum(v);
+}
+
 template <typename T>
 __device__ __forceinline__ void tridiag_cluster_onchip(cg::cluster_group &cluster, const MolDesc &md,
-                                                       const Work &w, T *sm, T *red, T *nrm2, T *kp2) {
+                                                       const Work &w, T *sm, T (*nrmw)[kClWarps],
+                                                       T (*kpw)[kClWarps]) {
   const int rank = (int)cluster.block_rank();
   const int n = md.nao;
   const int nloc = (n - rank + kClusterSize - 1) / kClusterSize;  // rows rank, rank + 8, ...
@@ -768,6 +789,19 @@ __device__ __forceinline__ void tridiag_cluster_onchip(cg::cluster_group &cluste
     const T *base = cluster.map_shared_rank(rows, i % kClusterSize);
     return base[(size_t)(i / kClusterSize) * n + j];
   };
+  // per-warp partial norm of column c over own rows i >= c + 2, published in buffer b
+  auto publish_norm = [&](int c, int b, int lfirst) {
+    T part = T(0);
+    for (int li = lfirst + lane + 32 * wid; li < nloc; li += 32 * nw) {
+      const int i = rank + li * kClusterSize;
+      if (i >= c + 2) {
+        const T x = rows[(size_t)li * n + c];
+        part += x * x;
+      }
+    }
+    part = warp_sum(part);
+    if (lane == 0) nrmw[b][wid] = part;
+  };
   // load own rows
   for (int li = wid; li < nloc; li += nw) {
     const T *src = Ag + (int64_t)(rank + li * kClusterSize) * n;
@@ -775,26 +809,13 @@ __device__ __forceinline__ void tridiag_cluster_onchip(cg::cluster_group &cluste
     for (int j = lane; j < n; j += 32) dst[j] = src[j];
   }
   __syncthreads();
-  // partial norm of column 0 over own rows i >= 2
-  {
-    T part = T(0);
-    for (int li = threadIdx.x; li < nloc; li += blockDim.x) {
-      const int i = rank + li * kClusterSize;
-      if (i >= 2) {
-        const T x = rows[(size_t)li * n];
-        part += x * x;
-      }
-    }
-    part = block_sum(part, red);
-    if (threadIdx.x == 0) nrm2[0] = part;
-  }
+  publish_norm(0, 0, 0);
   cluster.sync();
   for (int k = 0; k + 2 < n; ++k) {
     const int m1 = n - k - 1;
     const int buf = k & 1;
     // (a) reflector
-    T xn2 = T(0);
-    for (int r = 0; r < kClusterSize; ++r) xn2 += cluster.map_shared_rank(nrm2, r)[buf];
+    const T xn2 = cluster_partial_sum(cluster, nrmw, buf);
     const T alpha = remote(k + 1, k);
     T tk = T(0), scale = T(0), beta = alpha;
     if (xn2 != T(0)) {
@@ -812,16 +833,7 @@ __device__ __forceinline__ void tridiag_cluster_onchip(cg::cluster_group &cluste
                            ? (k + 1 - rank + kClusterSize - 1) / kClusterSize : 0;
     if (tk == T(0)) {
       // no reflection: publish the partial norm of column k + 1 and go on
-      T part = T(0);
-      for (int li = lfirst + threadIdx.x; li < nloc; li += blockDim.x) {
-        const int i = rank + li * kClusterSize;
-        if (i >= k + 3) {
-          const T x = rows[(size_t)li * n + k + 1];
-          part += x * x;
-        }
-      }
-      part = block_sum(part, red);
-      if (threadIdx.x == 0) nrm2[buf ^ 1] = part;
+      publish_norm(k + 1, buf ^ 1, lfirst);
       cluster.sync();
       continue;
     }
@@ -829,7 +841,7 @@ __device__ __forceinline__ void tridiag_cluster_onchip(cg::cluster_group &cluste
     __syncthreads();
     if (rank == 0)
       for (int t = threadIdx.x; t < m1; t += blockDim.x) Ag[(int64_t)k * n + k + 1 + t] = vs[t];
-    // (b) p = tau A22 v for own rows (warp per row), partial p.v
+    // (b) p = tau A22 v for own rows (warp per row), per-warp partial p.v
     T pv = T(0);
     for (int li = lfirst + wid; li < nloc; li += nw) {
       const int t = rank + li * kClusterSize - (k + 1);
@@ -842,12 +854,10 @@ __device__ __forceinline__ void tridiag_cluster_onchip(cg::cluster_group &cluste
         pv += acc * vs[t];
       }
     }
-    pv = block_sum(pv, red);
-    if (threadIdx.x == 0) kp2[buf] = pv;
+    if (lane == 0) kpw[buf][wid] = pv;
     cluster.sync();
     // (c) w for all rows
-    T K = T(0);
-    for (int r = 0; r < kClusterSize; ++r) K += cluster.map_shared_rank(kp2, r)[buf];
+    const T K = cluster_partial_sum(cluster, kpw, buf);
     const T half = T(0.5) * tk * K;
     for (int t = threadIdx.x; t < m1; t += blockDim.x) {
       const int i = k + 1 + t;
@@ -855,7 +865,7 @@ __device__ __forceinline__ void tridiag_cluster_onchip(cg::cluster_group &cluste
       wv[t] = p - half * vs[t];
     }
     __syncthreads();
-    // (d) rank-2 update of own rows, partial norm of column k + 1
+    // (d) rank-2 update of own rows, per-warp partial norm of column k + 1
     T part = T(0);
     for (int li = lfirst + wid; li < nloc; li += nw) {
       const int t = rank + li * kClusterSize - (k + 1);
@@ -864,11 +874,10 @@ __device__ __forceinline__ void tridiag_cluster_onchip(cg::cluster_group &cluste
       for (int j = lane; j < m1; j += 32) {
         const T a = row[j] - (vi * wv[j] + wi * vs[j]);
         row[j] = a;
-        if (j == 0 && t >= 2) part += a * a;  // column k + 1, rows k + 3 ...
+        if (j == 0 && t >= 2) part += a * a;  // column k + 1, rows k + 3 ... (lane 0)
       }
     }
-    part = block_sum(part, red);
-    if (threadIdx.x == 0) nrm2[buf ^ 1] = part;
+    if (lane == 0) nrmw[buf ^ 1][wid] = part;
     cluster.sync();
   }
   if (rank == 0 && threadIdx.x == 0) {
@@ -901,8 +910,7 @@ __global__ void __cluster_dims__(kClusterSize, 1, 1) __launch_bounds__(kTrdClThr
   if (m < 0) return;  // the whole cluster
   const MolDesc md = pl.mol[m];
   extern __shared__ double sm[];
-  __shared__ double red[32];
-  __shared__ double nrm2[2], kp2[2];
+  __shared__ double nrmw[2][kClWarps], kpw[2][kClWarps];
   // uniform over the cluster; FP32 passes of molecules that fit in shared
   // memory run in k_tridiag_smem (in the tail of a batch only those up to
   // kTailClusterMinN AOs), molecules above kClusterBlockedMinN AOs in
@@ -914,11 +922,11 @@ __global__ void __cluster_dims__(kClusterSize, 1, 1) __launch_bounds__(kTrdClThr
   const bool done = (w.phase[m] == kPhaseDone) || smem32 || md.nao > kClusterBlockedMinN || other_launch;
   if (!done) {
     if (w.prec[m])
-      tridiag_cluster_onchip<double>(cluster, md, w, sm, red, nrm2, kp2);
+      tridiag_cluster_onchip<double>(cluster, md, w, sm, nrmw, kpw);
     else
       tridiag_cluster_onchip<float>(cluster, md, w, reinterpret_cast<float *>(sm),
-                                    reinterpret_cast<float *>(red), reinterpret_cast<float *>(nrm2),
-                                    reinterpret_cast<float *>(kp2));
+                                    reinterpret_cast<float(*)[kClWarps]>(nrmw),
+                                    reinterpret_cast<float(*)[kClWarps]>(kpw));
   }
   // no CTA leaves while others may still read its shared memory
   cluster.sync();
