@@ -393,7 +393,7 @@ def run_serve(args, rank: int, world: int, local: int) -> None:
     nreq = args.serve_requests
     mols = molgen.c4_stream(nreq)
     evict = args.serve_evict if args.serve_evict > 0 else None
-    srv = Server(opts=OPTS, memory_gb=24.0, evict_after=evict)
+    srv = Server(opts=OPTS, memory_gb=24.0, evict_after=evict, straggler_share=args.serve_straggler_share)
     # warm-up: a few molecules of every size class
     for num, pos in sorted(mols, key=lambda m: len(m[0]))[:: max(1, nreq // 8)]:
         srv.submit(num, pos)
@@ -418,10 +418,24 @@ def run_serve(args, rank: int, world: int, local: int) -> None:
                     continue
                 srv.step()
             t_end = max(r.t_done for r in srv.completed)
+            # steady state: the completions between the 10th and the 90th
+            # percentile of the run, over the time between them (the ramp-up
+            # and the last stragglers left out)
+            done_t = np.sort([r.t_done for r in srv.completed])
+            lo, hi = int(0.1 * nreq), max(int(0.9 * nreq) - 1, int(0.1 * nreq) + 1)
+            steady = (hi - lo) / (done_t[hi] - done_t[lo]) if done_t[hi] > done_t[lo] else None
             lat = latency_summary(srv.completed)
             conv = sum(1 for r in srv.completed if r.status == 0)
             ev = sum(1 for r in srv.completed if r.evicted)
-            sweep.append({"rate_req_s": rate, "throughput": nreq / (t_end - t0), **lat, "converged": conv,
+            by_class = []
+            for c, pool in enumerate(srv.pools):
+                rs = [r for r in srv.completed if r.size_class == c]
+                if rs:
+                    by_class.append({"max_atoms": pool.max_atoms, "requests": len(rs), **latency_summary(rs),
+                                     "mean_passes": float(np.mean([r.iterations + 1 for r in rs])),
+                                     "evicted": sum(1 for r in rs if r.evicted)})
+            sweep.append({"rate_req_s": rate, "throughput": nreq / (t_end - t0), "steady_10_90": steady,
+                          "by_class": by_class, **lat, "converged": conv,
                           "evicted_stragglers": ev, "steps": srv.steps})
     # plain one-at-a-time path over the same molecules (a size-matched sample)
     sample = [mols[i] for i in size_matched(mols, min(24, nreq))]
@@ -444,7 +458,7 @@ def run_serve(args, rank: int, world: int, local: int) -> None:
                                f"{len(srv.pools)} size-class slot pools",
                    "pools": [{"max_atoms": p.max_atoms, "slots": p.nslots} for p in srv.pools],
                    "straggler_pools": [{"max_atoms": p.max_atoms, "slots": p.nslots} for p in srv.slow],
-                   "evict_after_passes": evict,
+                   "evict_after_passes": evict, "straggler_share": args.serve_straggler_share,
                    "device_bytes": srv.device_bytes},
         "served": sweep,
         "plain_per_molecule": {"value": plain, "unit": UNIT,
@@ -478,6 +492,8 @@ def main() -> None:
     ap.add_argument("--serve-rates", default="100,200,500,1000,2000,5000", help="arrival rates (req/s)")
     ap.add_argument("--serve-evict", type=int, default=60,
                     help="passes after which a served molecule moves to a straggler pool (0: never)")
+    ap.add_argument("--serve-straggler-share", type=float, default=0.15,
+                    help="straggler pool slots as a share of each class's main slots")
     ap.add_argument("--large", type=int, default=0, metavar="K",
                     help="large molecules instead of the batch: K of the 16 molecules of 1000-2000 atoms")
     ap.add_argument("--large-atoms", default="", metavar="N1,N2",
