@@ -16,8 +16,9 @@ smallest class whose atom, shell and orbital capacity it fits; one that fits
 no class is refused at submission.
 
 Stragglers: with ``evict_after`` set, a molecule still iterating after that
-many passes leaves its slot (``gbxtb_pool_evict``) and is solved again from
-the start in a small pool of the same class reserved for such molecules.
+many passes leaves its slot (``gbxtb_pool_evict``) when a queued request
+waits for a slot of its class, and is solved again from the start in a
+small pool of the same class reserved for such molecules.
 A fresh SCF of the same molecule takes the same path, so its result is the
 one it would have had; the main slots stop being held for up to ``maxiter``
 passes by molecules that converge slowly or not at all.
@@ -92,6 +93,7 @@ class Request:
     size_class: int | None = None
     passes: int = 0        # SCF passes run in its current slot
     evicted: bool = False  # moved to a straggler pool
+    dims: tuple[int, int] | None = None  # (shells, AOs)
 
     @property
     def latency(self) -> float | None:
@@ -127,7 +129,9 @@ class _Pool:
         return int(self.lib.gbxtb_pool_free_slots(self.handle))
 
     def fits(self, req: Request) -> bool:
-        nsh, nao = molecule_size(req.numbers)
+        if req.dims is None:
+            req.dims = molecule_size(req.numbers)
+        nsh, nao = req.dims
         return len(req.numbers) <= self.max_atoms and nsh <= self.cap_sh and nao <= self.cap_ao
 
     def evict(self, slot: int) -> Request:
@@ -249,7 +253,7 @@ class Server:
             raise ValueError(f"molecule with {len(num)} atoms, {nsh} shells and {nao} orbitals exceeds the "
                              f"largest size class ({big.max_atoms} atoms, {big.cap_sh} shells, {big.cap_ao} orbitals)")
         req = Request(self._next_id, num, np.asarray(positions, dtype=np.float64), float(charge), spin,
-                      time.perf_counter() if t_submit is None else t_submit)
+                      time.perf_counter() if t_submit is None else t_submit, dims=(nsh, nao))
         self._next_id += 1
         self.queue.append(req)
         return req
@@ -283,12 +287,34 @@ class Server:
 
     def _evict_stragglers(self, pool: "_Pool") -> None:
         """After a finished step of a main pool: molecules that have run
-        evict_after passes there move to the straggler pools."""
-        for slot, req in list(pool.requests.items()):
+        evict_after passes there move to the straggler pools, but only as
+        many as queued requests that fit this pool need slots beyond its
+        free ones, longest-running first.  A molecule with nothing waiting
+        for its slot keeps it (an evicted molecule starts again from the
+        guess, so eviction without a waiting request only costs passes)."""
+        for req in pool.requests.values():
             req.passes += 1
-            if self.evict_after and req.passes >= self.evict_after:
-                self.slow_queue.append(pool.evict(slot))
-                req.evicted = True
+        if not self.evict_after:
+            return
+        # queued requests that the next admission leaves waiting and that
+        # this pool could take (admission places a request in the first
+        # class that fits it and has a free slot)
+        free = [p.free() for p in self.pools]
+        need = 0
+        for r in self.queue:
+            c = next((c for c, p in enumerate(self.pools) if free[c] > 0 and p.fits(r)), None)
+            if c is not None:
+                free[c] -= 1
+            elif pool.fits(r):
+                need += 1
+        if need <= 0:
+            return
+        slow = sorted(((req.passes, slot) for slot, req in pool.requests.items() if req.passes >= self.evict_after),
+                      reverse=True)
+        for _, slot in slow[:need]:
+            req = pool.evict(slot)
+            req.evicted = True
+            self.slow_queue.append(req)
 
     def step(self, wait: bool = True) -> list[Request]:
         """Advance every pool at its own pace: collect the pools whose step

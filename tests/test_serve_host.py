@@ -174,16 +174,41 @@ def test_request_that_fits_no_class_by_orbitals_is_refused():
 
 
 def test_stragglers_move_to_the_straggler_pool():
-    """With evict_after = 3 passes and molecules needing 5, every molecule
-    leaves its main slot after 3 passes, restarts in the straggler pool and
-    finishes there; the main slot takes the next request meanwhile."""
+    """With evict_after = 3 passes and molecules needing 5: the first
+    molecule leaves its main slot after 3 passes because the second waits
+    for it, restarts in the straggler pool and finishes there; the second
+    takes the main slot meanwhile and, with nothing waiting behind it, keeps
+    it to the end."""
     srv = _server_with_fake_pools([(40, 1)], evict_after=3, slow=[(40, 1)], passes=5)
     for n in (5, 6):
         srv.submit(np.ones(n, dtype=np.int64), np.zeros((n, 3)))
     srv.run_until_idle()
     assert srv.idle
     assert sorted(r.id for r in srv.completed) == [0, 1]
-    assert all(r.evicted and r.status == 0 for r in srv.completed)
-    # request 1 entered the main slot while request 0 finished in the straggler pool
     by_id = {r.id: r for r in srv.completed}
+    assert by_id[0].evicted and not by_id[1].evicted
+    assert all(r.status == 0 for r in srv.completed)
+    # request 1 entered the main slot while request 0 finished in the straggler pool
     assert by_id[1].t_admit < by_id[0].t_done
+
+
+def test_eviction_only_for_waiting_requests():
+    """Three long molecules in three slots, two requests waiting: the two
+    longest-running stragglers leave (one per waiting request), the third
+    keeps its slot; a waiting request of another class evicts nothing."""
+    srv = _server_with_fake_pools([(10, 1), (40, 3)], evict_after=2, slow=[(10, 1), (40, 3)], passes=50)
+    for n in (30, 31, 32):
+        srv.submit(np.ones(n, dtype=np.int64), np.zeros((n, 3)))
+    srv.step(wait=False)
+    for _ in range(3):
+        srv.step(wait=False)
+    assert not any(r.evicted for p in srv.pools for r in p.requests.values())
+    srv.pools[1].requests[0].passes += 1  # slot 0 has run longest
+    srv.submit(np.ones(5, dtype=np.int64), np.zeros((5, 3)))  # small class: free slot
+    srv.submit(np.ones(33, dtype=np.int64), np.zeros((33, 3)))
+    srv.submit(np.ones(34, dtype=np.int64), np.zeros((34, 3)))
+    srv.step(wait=False)
+    evicted = sorted(r.id for r in srv.slow_queue) + sorted(r.id for p in srv.slow for r in p.requests.values())
+    assert evicted == [0, 1] or evicted == [0, 2]
+    assert 0 in evicted
+    assert sum(1 for r in srv.pools[1].requests.values() if r.id in (0, 1, 2)) == 1
