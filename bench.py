@@ -673,10 +673,12 @@ def main() -> None:
     g = C.c_double()
     _lib.check(lib.gbxtb_fp64_peak(C.byref(g)))
     fp64_peak = g.value / 1e3  # TFLOP/s
+    _lib.check(lib.gbxtb_fp64_mma_peak(C.byref(g)))
     roof = {"bound": "fp64", "kernel": dominant, "achieved": None, "peak": fp64_peak, "unit": "TFLOP/s",
             "frac": None, "traffic": None,
             "peak_source": "measured FP64 FMA microbenchmark (gbxtb_fp64_peak) in this run; "
-                           "MEASURED_PEAKS.json holds no FP64 figure"}
+                           "MEASURED_PEAKS.json holds no FP64 figure",
+            "fp64_mma_tflops": g.value / 1e3}
     if dominant in fl and per_step_ms[dominant] > 0:
         f64, f32 = fl[dominant]
         achieved = (f64 + f32 / FP32_PER_FP64) / (per_step_ms[dominant] * 1e-3) / 1e12

@@ -25,7 +25,7 @@ EXPORTED = (
     "gbxtb_plan_create", "gbxtb_plan_destroy", "gbxtb_plan_sizes", "gbxtb_integrals",
     "gbxtb_singlepoint", "gbxtb_get_status", "gbxtb_get_shell_potential", "gbxtb_get_orbital_charges",
     "gbxtb_get_profile",
-    "gbxtb_fp64_peak", "gbxtb_get_fp32_passes", "gbxtb_singlepoint_noalloc",
+    "gbxtb_fp64_peak", "gbxtb_fp64_mma_peak", "gbxtb_get_fp32_passes", "gbxtb_singlepoint_noalloc",
     "gbxtb_pool_create", "gbxtb_pool_destroy", "gbxtb_pool_free_slots", "gbxtb_pool_admit",
     "gbxtb_pool_step_launch", "gbxtb_pool_step_finish", "gbxtb_pool_result", "gbxtb_pool_step_poll",
     "gbxtb_plan_autotune", "gbxtb_default_options", "gbxtb_forces", "gbxtb_pool_evict",
@@ -149,6 +149,8 @@ def load() -> C.CDLL:
     lib.gbxtb_pool_result.argtypes = [vp, C.c_int32, f64p, f64p, f64p, i32p, i32p]
     lib.gbxtb_fp64_peak.argtypes = [C.POINTER(C.c_double)]
     lib.gbxtb_fp64_peak.restype = C.c_int
+    lib.gbxtb_fp64_mma_peak.argtypes = [C.POINTER(C.c_double)]
+    lib.gbxtb_fp64_mma_peak.restype = C.c_int
     lib.gbxtb_get_profile.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     for name in ("gbxtb_ctx_create", "gbxtb_plan_create", "gbxtb_plan_sizes", "gbxtb_integrals",
                  "gbxtb_singlepoint", "gbxtb_get_status", "gbxtb_get_shell_potential", "gbxtb_get_profile",

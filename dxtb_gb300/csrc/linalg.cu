@@ -733,51 +733,73 @@ __device__ __forceinline__ T ld_cg(const T *p) {
 // cluster keep their own rows (row i on CTA i mod 8, full length n) in
 // shared memory for the whole tridiagonalisation, so that the matrix-vector
 // product and the rank-2 update of a step touch only local shared memory.
-// Everything a CTA needs from the others is pushed to it before a cluster
-// barrier (stores to distributed shared memory, made visible by the
-// barrier's release/acquire), so no step waits on a remote load.  A step
-// has two cluster barriers and one CTA barrier:
-//   (a) every warp sums the 64 per-warp partial norms of column k (8 CTAs x
-//       8 warps, pushed to every CTA) and builds the reflector from column
-//       k, which the owners of its rows pushed to every CTA;
+//
+// The FP64 pipe of this GPU retires two FMAs per clock per SM (1/64 of the
+// FP32 rate), and an FP64 warp instruction holds it for 16 clocks whatever
+// its active lanes; a step is therefore laid out to issue as few FP64 warp
+// instructions as it can, more than to save latency:
+//   (a) warp 0 sums the 64 per-warp partial norms of column k (8 CTAs x 8
+//       warps), reads alpha from the owner of row k+1 and forms the
+//       reflector's scalars, which the other warps take from shared memory
+//       (one warp, not eight, runs the square root and the divisions);
+//       -- CTA barrier --  the CTA builds v from the owners' column
+//       entries (distributed shared memory);  -- CTA barrier --
+//   (b) p = tau A22 v for its own rows: a warp takes four rows at a time
+//       and sums their four dot products over the lanes together (six FP64
+//       adds by a transposed butterfly instead of twenty); per-warp
+//       partials of p.v are published;  -- cluster barrier 1 --
+//   (c) warp 0 sums the 64 partials of p.v;  -- CTA barrier --  the CTA
+//       gathers p from the owners and forms w = p - tau/2 (p.v) v;
 //       -- CTA barrier --
-//   (b) p = tau A22 v for its own rows (a warp per row, four rows at a time)
-//       pushed to every CTA, with per-warp partials of p.v;
-//       -- cluster barrier 1 --
-//   (c) every warp sums the 64 partials of p.v, and
-//   (d) A22 -= v w^T + w v^T on its own rows, w = p - tau/2 (p.v) v formed
-//       on the fly; the new column k + 1 of its rows and the per-warp
-//       partial norm of it are pushed to every CTA.
-//       -- cluster barrier 2 --
-// Every warp of every CTA sums the same 64 partials in the same order (a
-// fixed lane assignment and butterfly) and forms w from the same p, so tau,
-// beta, the scale and w are bitwise the same everywhere and every branch on
-// them is uniform over the cluster.  A buffer is rewritten only after a
-// cluster barrier that follows its last read (a step without reflection
-// adds one barrier for that).
+//   (d) A22 -= v w^T + w v^T on its own rows (two FMAs per element), with
+//       the per-warp partial norm of column k+1 accumulated on the fly and
+//       published.  -- cluster barrier 2 --
+// Every CTA sums the same 64 partials in the same order (a fixed lane
+// assignment and butterfly), so tau, beta, the scale and w are bitwise the
+// same everywhere and every branch on them is uniform over the cluster.
+// Partials are double-buffered by the parity of k: a buffer is rewritten
+// only after a barrier that follows its last read.
 // Output conventions as tridiag_body (reflector k in row k of A in global
 // memory, d, e, tau).
 constexpr int kClWarps = kTrdClThreads / 32;  // warps per CTA of the cluster kernels
 
-// Sum of the 64 per-warp partials part[0..64) (every CTA's, pushed here);
-// every lane of the calling warp gets the sum.
+// Sum over the cluster of the per-warp partials part[buf][0..kClWarps)
+// published by every CTA; every lane of the calling warp gets the sum.
 template <typename T>
-__device__ __forceinline__ T cluster_partial_sum(const T *part) {
+__device__ __forceinline__ T cluster_partial_sum(cg::cluster_group &cluster, T (*part)[kClWarps], int buf) {
   static_assert(kClusterSize * kClWarps == 64, "two partials per lane");
   const int lane = threadIdx.x & 31;
-  return warp_sum(part[lane] + part[lane + 32]);
+  T v = T(0);
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int idx = lane + 32 * h;
+    v += cluster.map_shared_rank(&part[buf][0], idx / kClWarps)[idx % kClWarps];
+  }
+  return warp_sum(v);
 }
 
-// Store x at p in the shared memory of every CTA of the cluster.
+// Sums of four per-lane values a0..a3 over the warp by a transposed
+// butterfly: after it, lane 8 q holds the sum of a_q (q = 0..3).
 template <typename T>
-__device__ __forceinline__ void push_all(cg::cluster_group &cluster, T *p, T x) {
+__device__ __forceinline__ T warp_sum4(T a0, T a1, T a2, T a3) {
+  const int lane = threadIdx.x & 31;
+  const bool h4 = lane & 16, h3 = lane & 8;
+  // offset 16: the lower half keeps rows 0, 1, the upper half rows 2, 3
+  const T s0 = h4 ? a0 : a2, s1 = h4 ? a1 : a3;
+  const T k0 = h4 ? a2 : a0, k1 = h4 ? a3 : a1;
+  const T b0 = k0 + __shfl_xor_sync(0xffffffffu, s0, 16);
+  const T b1 = k1 + __shfl_xor_sync(0xffffffffu, s1, 16);
+  // offset 8: bit 3 picks the first or the second row of the pair
+  T c = (h3 ? b1 : b0) + __shfl_xor_sync(0xffffffffu, h3 ? b0 : b1, 8);
 #pragma unroll
-  for (int r = 0; r < kClusterSize; ++r) *cluster.map_shared_rank(p, r) = x;
+  for (int off = 4; off > 0; off >>= 1) c += __shfl_xor_sync(0xffffffffu, c, off);
+  return c;
 }
 
 template <typename T>
 __device__ __forceinline__ void tridiag_cluster_onchip(cg::cluster_group &cluster, const MolDesc &md,
-                                                       const Work &w, T *sm, T *nrm, T *kp) {
+                                                       const Work &w, T *sm, T (*nrmw)[kClWarps],
+                                                       T (*kpw)[kClWarps], T *scal) {
   const int rank = (int)cluster.block_rank();
   const int n = md.nao;
   const int nloc = (n - rank + kClusterSize - 1) / kClusterSize;  // rows rank, rank + 8, ...
@@ -786,23 +808,26 @@ __device__ __forceinline__ void tridiag_cluster_onchip(cg::cluster_group &cluste
   T *rows = sm;                                   // [nloc_max][n]
   const int nloc_max = (n + kClusterSize - 1) / kClusterSize;
   T *vs = rows + (size_t)nloc_max * n;            // [n] reflector
-  T *col = vs + n;                                // [n] column k (by row), pushed by the owners
-  T *pf = col + n;                                // [n] p (by row), pushed by the owners
+  T *wv = vs + n;                                 // [n] w of all rows
+  T *ps = wv + n;                                 // [nloc_max] p of own rows (read by all)
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  // push column c of the own rows i >= c + 1 and the per-warp partial norm
-  // over i >= c + 2 (rows from local index lfirst on)
-  auto publish_col = [&](int c, int lfirst) {
+  // element (i, j) of the matrix in its owner's shared memory
+  auto remote = [&](int i, int j) -> T {
+    const T *base = cluster.map_shared_rank(rows, i % kClusterSize);
+    return base[(size_t)(i / kClusterSize) * n + j];
+  };
+  // per-warp partial norm of column c over own rows i >= c + 2, published in buffer b
+  auto publish_norm = [&](int c, int b, int lfirst) {
     T part = T(0);
     for (int li = lfirst + lane + 32 * wid; li < nloc; li += 32 * nw) {
       const int i = rank + li * kClusterSize;
-      if (i >= c + 1) {
+      if (i >= c + 2) {
         const T x = rows[(size_t)li * n + c];
-        push_all(cluster, col + i, x);
-        if (i >= c + 2) part += x * x;
+        part += x * x;
       }
     }
     part = warp_sum(part);
-    if (lane == 0) push_all(cluster, nrm + rank * kClWarps + wid, part);
+    if (lane == 0) nrmw[b][wid] = part;
   };
   // load own rows
   for (int li = wid; li < nloc; li += nw) {
@@ -811,47 +836,52 @@ __device__ __forceinline__ void tridiag_cluster_onchip(cg::cluster_group &cluste
     for (int j = lane; j < n; j += 32) dst[j] = src[j];
   }
   __syncthreads();
-  publish_col(0, 0);
+  publish_norm(0, 0, 0);
   cluster.sync();
   for (int k = 0; k + 2 < n; ++k) {
     const int m1 = n - k - 1;
-    // (a) reflector
-    const T xn2 = cluster_partial_sum(nrm);
-    const T alpha = col[k + 1];
-    T tk = T(0), scale = T(0), beta = alpha;
-    if (xn2 != T(0)) {
-      beta = -copysign(sqrt(alpha * alpha + xn2), alpha);
-      tk = (beta - alpha) / beta;
-      scale = T(1) / (alpha - beta);
-    }
-    if (threadIdx.x == 0) {
-      if (rank == 0) {
-        e[k] = beta;
-        tau[k] = tk;
+    const int buf = k & 1;
+    // (a) reflector scalars, by warp 0
+    if (wid == 0) {
+      const T xn2 = cluster_partial_sum(cluster, nrmw, buf);
+      const T alpha = remote(k + 1, k);
+      T tk = T(0), scale = T(0), beta = alpha;
+      if (xn2 != T(0)) {
+        beta = -copysign(sqrt(alpha * alpha + xn2), alpha);
+        tk = (beta - alpha) / beta;
+        scale = T(1) / (alpha - beta);
       }
-      if (rank == k % kClusterSize) d[k] = rows[(size_t)(k / kClusterSize) * n + k];
+      if (lane == 0) {
+        scal[0] = tk;
+        scal[1] = scale;
+        if (rank == 0) {
+          e[k] = beta;
+          tau[k] = tk;
+        }
+      }
+    } else if (threadIdx.x == 32 && rank == k % kClusterSize) {
+      d[k] = rows[(size_t)(k / kClusterSize) * n + k];
     }
+    __syncthreads();
+    const T tk = scal[0], scale = scal[1];
     // first own row at or after k + 1
     const int lfirst = (k + 1 - rank + kClusterSize - 1) / kClusterSize > 0
                            ? (k + 1 - rank + kClusterSize - 1) / kClusterSize : 0;
     if (tk == T(0)) {
-      // no reflection: once every CTA has read column k and its norm,
-      // push column k + 1 and go on
-      cluster.sync();
-      publish_col(k + 1, lfirst);
+      // no reflection: publish the partial norm of column k + 1 and go on
+      publish_norm(k + 1, buf ^ 1, lfirst);
       cluster.sync();
       continue;
     }
-    for (int t = threadIdx.x; t < m1; t += blockDim.x) vs[t] = (t == 0) ? T(1) : col[k + 1 + t] * scale;
+    for (int t = threadIdx.x; t < m1; t += blockDim.x) vs[t] = (t == 0) ? T(1) : remote(k + 1 + t, k) * scale;
     __syncthreads();
     if (rank == 0)
       for (int t = threadIdx.x; t < m1; t += blockDim.x) Ag[(int64_t)k * n + k + 1 + t] = vs[t];
-    // (b) p = tau A22 v for own rows, four rows of a warp at a time, pushed
-    // to every CTA; per-warp partial p.v
+    // (b) p = tau A22 v for own rows, four rows of a warp at a time; per-warp partial p.v
     T pv = T(0);
     for (int l0 = lfirst + wid; l0 < nloc; l0 += 4 * nw) {
       // rows l0, l0 + nw, l0 + 2 nw, l0 + 3 nw (past the end: row l0 again,
-      // result unused), with their four warp sums interleaved
+      // result unused)
       const int l1 = l0 + nw < nloc ? l0 + nw : l0, l2 = l0 + 2 * nw < nloc ? l0 + 2 * nw : l0,
                 l3 = l0 + 3 * nw < nloc ? l0 + 3 * nw : l0;
       const T *r0 = rows + (size_t)l0 * n + (k + 1), *r1 = rows + (size_t)l1 * n + (k + 1),
@@ -864,56 +894,58 @@ __device__ __forceinline__ void tridiag_cluster_onchip(cg::cluster_group &cluste
         a2 += r2[j] * vj;
         a3 += r3[j] * vj;
       }
-      a0 = warp_sum(a0);
-      a1 = warp_sum(a1);
-      a2 = warp_sum(a2);
-      a3 = warp_sum(a3);
-      const T acc[4] = {a0, a1, a2, a3};
+      const T c = warp_sum4(a0, a1, a2, a3) * tk;  // lane 8 q: p of row l0 + q nw
+      T pq[4];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int li = l0 + q * nw;
-        if (li < nloc) {
-          const int i = rank + li * kClusterSize;
-          const T pi = acc[q] * tk;
-          if (lane == q) push_all(cluster, pf + i, pi);  // four lanes store in parallel
-          pv += pi * vs[i - (k + 1)];
+      for (int q = 0; q < 4; ++q) pq[q] = __shfl_sync(0xffffffffu, c, 8 * q);
+      if (lane == 0) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int li = l0 + q * nw;
+          if (li < nloc) {
+            ps[li] = pq[q];
+            pv += pq[q] * vs[rank + li * kClusterSize - (k + 1)];
+          }
         }
       }
     }
-    if (lane == 0) push_all(cluster, kp + rank * kClWarps + wid, pv);
+    if (lane == 0) kpw[buf][wid] = pv;
     cluster.sync();
-    // (c) p.v, and (d) the rank-2 update of own rows with w formed on the
-    // fly; column k + 1 and its partial norm pushed to every CTA
-    const T half = T(0.5) * tk * cluster_partial_sum(kp);
-    const T *pk = pf + (k + 1);
+    // (c) p.v by warp 0, then w for all rows
+    if (wid == 0) {
+      const T K = cluster_partial_sum(cluster, kpw, buf);
+      if (lane == 0) scal[2] = T(0.5) * tk * K;
+    }
+    __syncthreads();
+    const T half = scal[2];
+    for (int t = threadIdx.x; t < m1; t += blockDim.x) {
+      const int i = k + 1 + t;
+      const T p = cluster.map_shared_rank(ps, i % kClusterSize)[i / kClusterSize];
+      wv[t] = p - half * vs[t];
+    }
+    __syncthreads();
+    // (d) rank-2 update of own rows, per-warp partial norm of column k + 1
     T part = T(0);
     for (int li = lfirst + wid; li < nloc; li += nw) {
       const int t = rank + li * kClusterSize - (k + 1);
       T *row = rows + (size_t)li * n + (k + 1);
-      const T vi = vs[t], wi = pk[t] - half * vi;
+      const T vi = vs[t], wi = wv[t];
       for (int j = lane; j < m1; j += 32) {
-        const T vj = vs[j];
-        const T a = row[j] - (vi * (pk[j] - half * vj) + wi * vj);
+        const T a = fma(-vi, wv[j], fma(-wi, vs[j], row[j]));
         row[j] = a;
-        if (j == 0 && t >= 1) {  // column k + 1, rows k + 2 ... (lane 0)
-          push_all(cluster, col + (k + 1 + t), a);
-          if (t >= 2) part += a * a;
-        }
+        if (j == 0 && t >= 2) part += a * a;  // column k + 1, rows k + 3 ... (lane 0)
       }
     }
-    if (lane == 0) push_all(cluster, nrm + rank * kClWarps + wid, part);
+    if (lane == 0) nrmw[buf ^ 1][wid] = part;
     cluster.sync();
   }
-  if (threadIdx.x == 0) {
-    auto own = [&](int i, int j) { return rows[(size_t)(i / kClusterSize) * n + j]; };
+  if (rank == 0 && threadIdx.x == 0) {
     if (n >= 2) {
-      if (rank == (n - 2) % kClusterSize) d[n - 2] = own(n - 2, n - 2);
-      if (rank == (n - 1) % kClusterSize) {
-        d[n - 1] = own(n - 1, n - 1);
-        e[n - 2] = own(n - 1, n - 2);
-      }
-    } else if (rank == 0) {
-      d[0] = own(0, 0);
+      d[n - 2] = remote(n - 2, n - 2);
+      d[n - 1] = remote(n - 1, n - 1);
+      e[n - 2] = remote(n - 1, n - 2);
+    } else {
+      d[0] = remote(0, 0);
     }
   }
 }
@@ -921,7 +953,7 @@ __device__ __forceinline__ void tridiag_cluster_onchip(cg::cluster_group &cluste
 // Shared memory of tridiag_cluster_onchip for n AOs.
 template <typename T>
 __host__ __device__ constexpr size_t onchip_smem_bytes(int n) {
-  return sizeof(T) * ((size_t)((n + kClusterSize - 1) / kClusterSize) * n + 3 * (size_t)n);
+  return sizeof(T) * ((size_t)((n + kClusterSize - 1) / kClusterSize) * (n + 1) + 2 * (size_t)n);
 }
 // Molecules whose rows need at most this much shared memory per CTA run in
 // a launch sized for it, which lets two CTAs share an SM (FP64 up to 320
@@ -937,7 +969,7 @@ __global__ void __cluster_dims__(kClusterSize, 1, 1) __launch_bounds__(kTrdClThr
   if (m < 0) return;  // the whole cluster
   const MolDesc md = pl.mol[m];
   extern __shared__ double sm[];
-  __shared__ double nrm[kClusterSize * kClWarps], kp[kClusterSize * kClWarps];
+  __shared__ double nrmw[2][kClWarps], kpw[2][kClWarps], scal[4];
   // uniform over the cluster; FP32 passes of molecules that fit in shared
   // memory run in k_tridiag_smem (in the tail of a batch only those up to
   // kTailClusterMinN AOs), molecules above kClusterBlockedMinN AOs in
@@ -949,10 +981,11 @@ __global__ void __cluster_dims__(kClusterSize, 1, 1) __launch_bounds__(kTrdClThr
   const bool done = (w.phase[m] == kPhaseDone) || smem32 || md.nao > kClusterBlockedMinN || other_launch;
   if (!done) {
     if (w.prec[m])
-      tridiag_cluster_onchip<double>(cluster, md, w, sm, nrm, kp);
+      tridiag_cluster_onchip<double>(cluster, md, w, sm, nrmw, kpw, scal);
     else
-      tridiag_cluster_onchip<float>(cluster, md, w, reinterpret_cast<float *>(sm), reinterpret_cast<float *>(nrm),
-                                    reinterpret_cast<float *>(kp));
+      tridiag_cluster_onchip<float>(cluster, md, w, reinterpret_cast<float *>(sm),
+                                    reinterpret_cast<float(*)[kClWarps]>(nrmw),
+                                    reinterpret_cast<float(*)[kClWarps]>(kpw), reinterpret_cast<float *>(scal));
   }
   // no CTA leaves while others may still read its shared memory
   cluster.sync();

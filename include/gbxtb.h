@@ -364,6 +364,12 @@ GBXTB_API int gbxtb_singlepoint_noalloc(gbxtb_plan *plan, const gbxtb_options *o
  * FP64-bound kernels.  No counterpart in the reference. */
 GBXTB_API int gbxtb_fp64_peak(double *gflops);
 
+/* Measured FP64 tensor-core (warp-level m8n8k4 MMA) throughput of the
+ * current device in GFLOP/s (a short microbenchmark): whether FP64 panel
+ * updates would run faster as MMA than as FMA.  No counterpart in the
+ * reference. */
+GBXTB_API int gbxtb_fp64_mma_peak(double *gflops);
+
 #ifdef __cplusplus
 }
 #endif

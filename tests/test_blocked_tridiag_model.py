@@ -117,28 +117,20 @@ def test_blocked_model_zero_column():
 
 def onchip_cluster_tridiag(a: np.ndarray, csize: int = 8):
     """Phase-by-phase model of tridiag_cluster_onchip (csrc/linalg.cu): rows
-    owned cyclically by `csize` CTAs in their shared memory; the owners push
-    column k of their rows and its partial norms to every CTA (the next
-    column during the update of the previous step), and p of their rows
-    with the partials of p.v; every CTA forms w on the fly in its update.
-    Returns d, e, tau and the reflector rows, in the kernel's index
-    conventions."""
+    owned cyclically by `csize` CTAs in their shared memory, partial column
+    norms published per CTA (the norm of column k+1 accumulated during the
+    update of step k), p of own rows gathered by every CTA.  Returns d, e,
+    tau and the reflector rows, in the kernel's index conventions."""
     n = a.shape[0]
     own = [[i for i in range(n) if i % csize == r] for r in range(csize)]
     rows = {i: a[i].copy() for i in range(n)}  # row i on CTA i % csize
     d, e, tau = np.zeros(n), np.zeros(n), np.zeros(n)
     refl = np.zeros((n, n))
-
-    def publish(c):
-        col = {i: rows[i][c] for r in range(csize) for i in own[r] if i >= c + 1}
-        nrm = [sum(rows[i][c] ** 2 for i in own[r] if i >= c + 2) for r in range(csize)]
-        return col, nrm
-
-    col, nrm = publish(0)
+    nrm = [sum(rows[i][0] ** 2 for i in own[r] if i >= 2) for r in range(csize)]
     for k in range(n - 2):
         m1 = n - k - 1
         xn2 = sum(nrm)
-        alpha = col[k + 1]
+        alpha = rows[k + 1][k]
         tk, scale, beta = 0.0, 0.0, alpha
         if xn2 != 0.0:
             beta = -np.copysign(np.sqrt(alpha * alpha + xn2), alpha)
@@ -146,30 +138,27 @@ def onchip_cluster_tridiag(a: np.ndarray, csize: int = 8):
             scale = 1.0 / (alpha - beta)
         d[k], e[k], tau[k] = rows[k][k], beta, tk
         if tk == 0.0:
-            col, nrm = publish(k + 1)
+            nrm = [sum(rows[i][k + 1] ** 2 for i in own[r] if i >= k + 3) for r in range(csize)]
             continue
-        v = np.array([1.0] + [col[k + 1 + t] * scale for t in range(1, m1)])
+        v = np.array([1.0] + [rows[k + 1 + t][k] * scale for t in range(1, m1)])
         refl[k, k + 1:] = v
-        pf, kp = {}, [0.0] * csize
+        ps, kp = {}, [0.0] * csize
         for r in range(csize):
             for i in own[r]:
                 if i < k + 1:
                     continue
                 t = i - (k + 1)
-                pf[i] = tk * np.dot(rows[i][k + 1:], v)
-                kp[r] += pf[i] * v[t]
+                ps[i] = tk * np.dot(rows[i][k + 1:], v)
+                kp[r] += ps[i] * v[t]
         half = 0.5 * tk * sum(kp)
-        p = np.array([pf[k + 1 + t] for t in range(m1)])
-        col, nrm = {}, [0.0] * csize
+        wv = np.array([ps[k + 1 + t] - half * v[t] for t in range(m1)])
+        nrm = [0.0] * csize
         for r in range(csize):
             for i in own[r]:
                 if i < k + 1:
                     continue
                 t = i - (k + 1)
-                wi = p[t] - half * v[t]
-                rows[i][k + 1:] -= v[t] * (p - half * v) + wi * v
-                if t >= 1:
-                    col[i] = rows[i][k + 1]
+                rows[i][k + 1:] -= v[t] * wv + wv[t] * v
                 if t >= 2:
                     nrm[r] += rows[i][k + 1] ** 2
     d[n - 2], d[n - 1], e[n - 2] = rows[n - 2][n - 2], rows[n - 1][n - 1], rows[n - 1][n - 2]

@@ -125,3 +125,17 @@ def test_two_iterations_end_unconverged():
     with warnings.catch_warnings():
         warnings.simplefilter("error")
         calc_for(num).get_energy(p)
+
+
+def test_fp64_throughput_probes():
+    """The FP64 FMA and FP64 MMA microbenchmarks run and report plausible
+    rates (between 10 GFLOP/s and 100 TFLOP/s)."""
+    import ctypes as C
+
+    from dxtb_gb300 import _lib
+
+    lib = _lib.load()
+    for probe in (lib.gbxtb_fp64_peak, lib.gbxtb_fp64_mma_peak):
+        g = C.c_double()
+        _lib.check(probe(C.byref(g)))
+        assert 1e1 < g.value < 1e5, g.value
