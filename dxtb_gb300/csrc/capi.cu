@@ -534,11 +534,12 @@ int enqueue_pass(gbxtb_plan *plan, const Work &w, const gbxtb_options &o, bool t
   if (opts->mixed_precision) launch_tridiag_smem(pl, w, s, tail);
   int ntrd = opts->mixed_precision ? plan->smem_launches : 0;
   if (tail) {
-    ntrd += launch_tridiag_cluster(pl, w, w.active_list, active, plan->maxn, s, true);
+    ntrd += launch_tridiag_cluster(pl, w, w.active_list, active, plan->maxn, s, true, opts->mixed_precision != 0);
   } else {
     // large FP64 passes and FP32 passes too large for shared memory on 8-SM
     // clusters, the rest one CTA per molecule
-    if (nclus > 0) ntrd += launch_tridiag_cluster(pl, w, w.cluster_list, nclus, plan->maxn, s);
+    if (nclus > 0)
+      ntrd += launch_tridiag_cluster(pl, w, w.cluster_list, nclus, plan->maxn, s, false, opts->mixed_precision != 0);
     launch_tridiag(pl, w, plan->maxn, s);
     ntrd += 1;
   }

@@ -35,6 +35,7 @@
 // the n x n double block); FP32 copies of L^-1 (with L^T above the
 // diagonal) and of L^-1 H0 L^-T are made once per geometry in w.lo.
 #include "internal.cuh"
+#include "df64.cuh"
 
 #include <cmath>
 #include <algorithm>
@@ -763,36 +764,119 @@ __device__ __forceinline__ T ld_cg(const T *p) {
 // memory, d, e, tau).
 constexpr int kClWarps = kTrdClThreads / 32;  // warps per CTA of the cluster kernels
 
+// Element arithmetic of tridiag_cluster_onchip.  T is the type the rows
+// are held and updated in (FP32 passes: float; FP64 passes: double, or
+// df64, double-float pairs on the FP32 pipe, in mixed-precision runs), G
+// the type of the matrix in global memory.  The float and double forms are
+// the plain expressions; the reflector's scalars of a df64 reduction are
+// formed in double.
+template <typename T>
+struct ClOps;
+
+template <typename R>
+struct ClOpsNative {
+  using G = R;
+  using Acc = R;
+  static __device__ __forceinline__ R zero() { return R(0); }
+  static __device__ __forceinline__ R one() { return R(1); }
+  static __device__ __forceinline__ R load(G x) { return x; }
+  static __device__ __forceinline__ G store(R x) { return x; }
+  static __device__ __forceinline__ double to_d(R x) { return (double)x; }
+  static __device__ __forceinline__ bool is_zero(R x) { return x == R(0); }
+  static __device__ __forceinline__ R add(R a, R b) { return a + b; }
+  static __device__ __forceinline__ R mul(R a, R b) { return a * b; }
+  static __device__ __forceinline__ R half_prod(R tk, R K) { return R(0.5) * tk * K; }
+  static __device__ __forceinline__ R axpy_neg(R p, R h, R v) { return p - h * v; }  // p - h v
+  static __device__ __forceinline__ R rank2(R a, R vi, R wj, R wi, R vj) { return fma(-vi, wj, fma(-wi, vj, a)); }
+  static __device__ __forceinline__ Acc acc0() { return R(0); }
+  static __device__ __forceinline__ void dot(Acc &acc, R a, R b) { acc += a * b; }
+  static __device__ __forceinline__ R fin(Acc acc) { return acc; }
+  static __device__ __forceinline__ R shfl_xor(R a, int off) { return __shfl_xor_sync(0xffffffffu, a, off); }
+  static __device__ __forceinline__ R shfl(R a, int src) { return __shfl_sync(0xffffffffu, a, src); }
+  // Householder scalars from the squared norm below alpha and alpha
+  static __device__ __forceinline__ void reflector(R xn2, R alpha, R &tk, R &scale, double &beta_out) {
+    R beta = alpha;
+    tk = R(0);
+    scale = R(0);
+    if (xn2 != R(0)) {
+      beta = -copysign(sqrt(alpha * alpha + xn2), alpha);
+      tk = (beta - alpha) / beta;
+      scale = R(1) / (alpha - beta);
+    }
+    beta_out = (double)beta;
+  }
+};
+template <>
+struct ClOps<float> : ClOpsNative<float> {};
+template <>
+struct ClOps<double> : ClOpsNative<double> {};
+
+template <>
+struct ClOps<df64> {
+  using G = double;
+  using Acc = DfAcc;
+  static __device__ __forceinline__ df64 zero() { return df64(0.f); }
+  static __device__ __forceinline__ df64 one() { return df64(1.f); }
+  static __device__ __forceinline__ df64 load(G x) { return df_from_double(x); }
+  static __device__ __forceinline__ G store(df64 x) { return df_to_double(x); }
+  static __device__ __forceinline__ double to_d(df64 x) { return df_to_double(x); }
+  static __device__ __forceinline__ bool is_zero(df64 x) { return x.hi == 0.f; }
+  static __device__ __forceinline__ df64 add(df64 a, df64 b) { return df_add(a, b); }
+  static __device__ __forceinline__ df64 mul(df64 a, df64 b) { return df_mul(a, b); }
+  static __device__ __forceinline__ df64 half_prod(df64 tk, df64 K) {
+    return df_mul(df64(0.5f * tk.hi, 0.5f * tk.lo), K);  // exact halving
+  }
+  static __device__ __forceinline__ df64 axpy_neg(df64 p, df64 h, df64 v) { return df_add(p, df_neg(df_mul(h, v))); }
+  static __device__ __forceinline__ df64 rank2(df64 a, df64 vi, df64 wj, df64 wi, df64 vj) {
+    return df_rank2(a, vi, wj, wi, vj);
+  }
+  static __device__ __forceinline__ Acc acc0() { return DfAcc{}; }
+  static __device__ __forceinline__ void dot(Acc &acc, df64 a, df64 b) { df_dot_add(acc, a, b); }
+  static __device__ __forceinline__ df64 fin(Acc acc) { return df_dot_final(acc); }
+  static __device__ __forceinline__ df64 shfl_xor(df64 a, int off) { return df_shfl_xor(a, off); }
+  static __device__ __forceinline__ df64 shfl(df64 a, int src) { return df_shfl(a, src); }
+  static __device__ __forceinline__ void reflector(df64 xn2, df64 alpha, df64 &tk, df64 &scale, double &beta_out) {
+    double t, sc;
+    ClOpsNative<double>::reflector(df_to_double(xn2), df_to_double(alpha), t, sc, beta_out);
+    tk = df_from_double(t);
+    scale = df_from_double(sc);
+  }
+};
+
+template <typename T>
+__device__ __forceinline__ T cl_warp_sum(T v) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v = ClOps<T>::add(v, ClOps<T>::shfl_xor(v, off));
+  return v;
+}
+
 // Sum over the cluster of the per-warp partials part[buf][0..kClWarps)
 // published by every CTA; every lane of the calling warp gets the sum.
 template <typename T>
 __device__ __forceinline__ T cluster_partial_sum(cg::cluster_group &cluster, T (*part)[kClWarps], int buf) {
   static_assert(kClusterSize * kClWarps == 64, "two partials per lane");
   const int lane = threadIdx.x & 31;
-  T v = T(0);
-#pragma unroll
-  for (int h = 0; h < 2; ++h) {
-    const int idx = lane + 32 * h;
-    v += cluster.map_shared_rank(&part[buf][0], idx / kClWarps)[idx % kClWarps];
-  }
-  return warp_sum(v);
+  const T v0 = cluster.map_shared_rank(&part[buf][0], lane / kClWarps)[lane % kClWarps];
+  const T v1 = cluster.map_shared_rank(&part[buf][0], (lane + 32) / kClWarps)[(lane + 32) % kClWarps];
+  return cl_warp_sum(ClOps<T>::add(ClOps<T>::add(ClOps<T>::zero(), v0), v1));
 }
 
 // Sums of four per-lane values a0..a3 over the warp by a transposed
 // butterfly: after it, lane 8 q holds the sum of a_q (q = 0..3).
 template <typename T>
 __device__ __forceinline__ T warp_sum4(T a0, T a1, T a2, T a3) {
+  using O = ClOps<T>;
   const int lane = threadIdx.x & 31;
   const bool h4 = lane & 16, h3 = lane & 8;
   // offset 16: the lower half keeps rows 0, 1, the upper half rows 2, 3
   const T s0 = h4 ? a0 : a2, s1 = h4 ? a1 : a3;
   const T k0 = h4 ? a2 : a0, k1 = h4 ? a3 : a1;
-  const T b0 = k0 + __shfl_xor_sync(0xffffffffu, s0, 16);
-  const T b1 = k1 + __shfl_xor_sync(0xffffffffu, s1, 16);
+  const T b0 = O::add(k0, O::shfl_xor(s0, 16));
+  const T b1 = O::add(k1, O::shfl_xor(s1, 16));
   // offset 8: bit 3 picks the first or the second row of the pair
-  T c = (h3 ? b1 : b0) + __shfl_xor_sync(0xffffffffu, h3 ? b0 : b1, 8);
+  T c = O::add(h3 ? b1 : b0, O::shfl_xor(h3 ? b0 : b1, 8));
 #pragma unroll
-  for (int off = 4; off > 0; off >>= 1) c += __shfl_xor_sync(0xffffffffu, c, off);
+  for (int off = 4; off > 0; off >>= 1) c = O::add(c, O::shfl_xor(c, off));
   return c;
 }
 
@@ -800,10 +884,13 @@ template <typename T>
 __device__ __forceinline__ void tridiag_cluster_onchip(cg::cluster_group &cluster, const MolDesc &md,
                                                        const Work &w, T *sm, T (*nrmw)[kClWarps],
                                                        T (*kpw)[kClWarps], T *scal) {
+  using O = ClOps<T>;
+  using G = typename O::G;
+  using Acc = typename O::Acc;
   const int rank = (int)cluster.block_rank();
   const int n = md.nao;
   const int nloc = (n - rank + kClusterSize - 1) / kClusterSize;  // rows rank, rank + 8, ...
-  T *Ag = mat_view<T>(w.A, md.mat0);
+  G *Ag = mat_view<G>(w.A, md.mat0);
   double *d = w.d + md.ao0, *e = w.e + md.ao0, *tau = w.tau + md.ao0;
   T *rows = sm;                                   // [nloc_max][n]
   const int nloc_max = (n + kClusterSize - 1) / kClusterSize;
@@ -818,22 +905,22 @@ __device__ __forceinline__ void tridiag_cluster_onchip(cg::cluster_group &cluste
   };
   // per-warp partial norm of column c over own rows i >= c + 2, published in buffer b
   auto publish_norm = [&](int c, int b, int lfirst) {
-    T part = T(0);
+    Acc part = O::acc0();
     for (int li = lfirst + lane + 32 * wid; li < nloc; li += 32 * nw) {
       const int i = rank + li * kClusterSize;
       if (i >= c + 2) {
         const T x = rows[(size_t)li * n + c];
-        part += x * x;
+        O::dot(part, x, x);
       }
     }
-    part = warp_sum(part);
-    if (lane == 0) nrmw[b][wid] = part;
+    const T sum = cl_warp_sum(O::fin(part));
+    if (lane == 0) nrmw[b][wid] = sum;
   };
   // load own rows
   for (int li = wid; li < nloc; li += nw) {
-    const T *src = Ag + (int64_t)(rank + li * kClusterSize) * n;
+    const G *src = Ag + (int64_t)(rank + li * kClusterSize) * n;
     T *dst = rows + (size_t)li * n;
-    for (int j = lane; j < n; j += 32) dst[j] = src[j];
+    for (int j = lane; j < n; j += 32) dst[j] = O::load(src[j]);
   }
   __syncthreads();
   publish_norm(0, 0, 0);
@@ -845,40 +932,37 @@ __device__ __forceinline__ void tridiag_cluster_onchip(cg::cluster_group &cluste
     if (wid == 0) {
       const T xn2 = cluster_partial_sum(cluster, nrmw, buf);
       const T alpha = remote(k + 1, k);
-      T tk = T(0), scale = T(0), beta = alpha;
-      if (xn2 != T(0)) {
-        beta = -copysign(sqrt(alpha * alpha + xn2), alpha);
-        tk = (beta - alpha) / beta;
-        scale = T(1) / (alpha - beta);
-      }
+      T tk, scale;
+      double beta;
+      O::reflector(xn2, alpha, tk, scale, beta);
       if (lane == 0) {
         scal[0] = tk;
         scal[1] = scale;
         if (rank == 0) {
           e[k] = beta;
-          tau[k] = tk;
+          tau[k] = O::to_d(tk);
         }
       }
     } else if (threadIdx.x == 32 && rank == k % kClusterSize) {
-      d[k] = rows[(size_t)(k / kClusterSize) * n + k];
+      d[k] = O::to_d(rows[(size_t)(k / kClusterSize) * n + k]);
     }
     __syncthreads();
     const T tk = scal[0], scale = scal[1];
     // first own row at or after k + 1
     const int lfirst = (k + 1 - rank + kClusterSize - 1) / kClusterSize > 0
                            ? (k + 1 - rank + kClusterSize - 1) / kClusterSize : 0;
-    if (tk == T(0)) {
+    if (O::is_zero(tk)) {
       // no reflection: publish the partial norm of column k + 1 and go on
       publish_norm(k + 1, buf ^ 1, lfirst);
       cluster.sync();
       continue;
     }
-    for (int t = threadIdx.x; t < m1; t += blockDim.x) vs[t] = (t == 0) ? T(1) : remote(k + 1 + t, k) * scale;
+    for (int t = threadIdx.x; t < m1; t += blockDim.x) vs[t] = (t == 0) ? O::one() : O::mul(remote(k + 1 + t, k), scale);
     __syncthreads();
     if (rank == 0)
-      for (int t = threadIdx.x; t < m1; t += blockDim.x) Ag[(int64_t)k * n + k + 1 + t] = vs[t];
+      for (int t = threadIdx.x; t < m1; t += blockDim.x) Ag[(int64_t)k * n + k + 1 + t] = O::store(vs[t]);
     // (b) p = tau A22 v for own rows, four rows of a warp at a time; per-warp partial p.v
-    T pv = T(0);
+    Acc pv = O::acc0();
     for (int l0 = lfirst + wid; l0 < nloc; l0 += 4 * nw) {
       // rows l0, l0 + nw, l0 + 2 nw, l0 + 3 nw (past the end: row l0 again,
       // result unused)
@@ -886,66 +970,67 @@ __device__ __forceinline__ void tridiag_cluster_onchip(cg::cluster_group &cluste
                 l3 = l0 + 3 * nw < nloc ? l0 + 3 * nw : l0;
       const T *r0 = rows + (size_t)l0 * n + (k + 1), *r1 = rows + (size_t)l1 * n + (k + 1),
               *r2 = rows + (size_t)l2 * n + (k + 1), *r3 = rows + (size_t)l3 * n + (k + 1);
-      T a0 = T(0), a1 = T(0), a2 = T(0), a3 = T(0);
+      Acc a0 = O::acc0(), a1 = O::acc0(), a2 = O::acc0(), a3 = O::acc0();
       for (int j = lane; j < m1; j += 32) {
         const T vj = vs[j];
-        a0 += r0[j] * vj;
-        a1 += r1[j] * vj;
-        a2 += r2[j] * vj;
-        a3 += r3[j] * vj;
+        O::dot(a0, r0[j], vj);
+        O::dot(a1, r1[j], vj);
+        O::dot(a2, r2[j], vj);
+        O::dot(a3, r3[j], vj);
       }
-      const T c = warp_sum4(a0, a1, a2, a3) * tk;  // lane 8 q: p of row l0 + q nw
+      // lane 8 q: p of row l0 + q nw
+      const T c = O::mul(warp_sum4(O::fin(a0), O::fin(a1), O::fin(a2), O::fin(a3)), tk);
       T pq[4];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) pq[q] = __shfl_sync(0xffffffffu, c, 8 * q);
+      for (int q = 0; q < 4; ++q) pq[q] = O::shfl(c, 8 * q);
       if (lane == 0) {
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           const int li = l0 + q * nw;
           if (li < nloc) {
             ps[li] = pq[q];
-            pv += pq[q] * vs[rank + li * kClusterSize - (k + 1)];
+            O::dot(pv, pq[q], vs[rank + li * kClusterSize - (k + 1)]);
           }
         }
       }
     }
-    if (lane == 0) kpw[buf][wid] = pv;
+    if (lane == 0) kpw[buf][wid] = O::fin(pv);
     cluster.sync();
     // (c) p.v by warp 0, then w for all rows
     if (wid == 0) {
       const T K = cluster_partial_sum(cluster, kpw, buf);
-      if (lane == 0) scal[2] = T(0.5) * tk * K;
+      if (lane == 0) scal[2] = O::half_prod(tk, K);
     }
     __syncthreads();
     const T half = scal[2];
     for (int t = threadIdx.x; t < m1; t += blockDim.x) {
       const int i = k + 1 + t;
       const T p = cluster.map_shared_rank(ps, i % kClusterSize)[i / kClusterSize];
-      wv[t] = p - half * vs[t];
+      wv[t] = O::axpy_neg(p, half, vs[t]);
     }
     __syncthreads();
     // (d) rank-2 update of own rows, per-warp partial norm of column k + 1
-    T part = T(0);
+    Acc part = O::acc0();
     for (int li = lfirst + wid; li < nloc; li += nw) {
       const int t = rank + li * kClusterSize - (k + 1);
       T *row = rows + (size_t)li * n + (k + 1);
       const T vi = vs[t], wi = wv[t];
       for (int j = lane; j < m1; j += 32) {
-        const T a = fma(-vi, wv[j], fma(-wi, vs[j], row[j]));
+        const T a = O::rank2(row[j], vi, wv[j], wi, vs[j]);
         row[j] = a;
-        if (j == 0 && t >= 2) part += a * a;  // column k + 1, rows k + 3 ... (lane 0)
+        if (j == 0 && t >= 2) O::dot(part, a, a);  // column k + 1, rows k + 3 ... (lane 0)
       }
     }
-    if (lane == 0) nrmw[buf ^ 1][wid] = part;
+    if (lane == 0) nrmw[buf ^ 1][wid] = O::fin(part);
     cluster.sync();
   }
   if (rank == 0 && threadIdx.x == 0) {
     if (n >= 2) {
-      d[n - 2] = remote(n - 2, n - 2);
-      d[n - 1] = remote(n - 1, n - 1);
-      e[n - 2] = remote(n - 1, n - 2);
+      d[n - 2] = O::to_d(remote(n - 2, n - 2));
+      d[n - 1] = O::to_d(remote(n - 1, n - 1));
+      e[n - 2] = O::to_d(remote(n - 1, n - 2));
     } else {
-      d[0] = remote(0, 0);
+      d[0] = O::to_d(remote(0, 0));
     }
   }
 }
@@ -963,7 +1048,7 @@ __host__ __device__ constexpr size_t onchip_smem_bytes(int n) {
 constexpr size_t kOnchipSmallBytes = 110 * 1024;
 
 __global__ void __cluster_dims__(kClusterSize, 1, 1) __launch_bounds__(kTrdClThreads)
-    k_tridiag_cluster(DevPlan pl, Work w, const int32_t *mol_list, int tail, int big) {
+    k_tridiag_cluster(DevPlan pl, Work w, const int32_t *mol_list, int tail, int big, int split64) {
   cg::cluster_group cluster = cg::this_cluster();
   const int m = list_mol(w, mol_list, blockIdx.x / kClusterSize);
   if (m < 0) return;  // the whole cluster
@@ -980,7 +1065,11 @@ __global__ void __cluster_dims__(kClusterSize, 1, 1) __launch_bounds__(kTrdClThr
   const bool other_launch = big ? need <= kOnchipSmallBytes : need > kOnchipSmallBytes;
   const bool done = (w.phase[m] == kPhaseDone) || smem32 || md.nao > kClusterBlockedMinN || other_launch;
   if (!done) {
-    if (w.prec[m])
+    if (w.prec[m] && split64)
+      tridiag_cluster_onchip<df64>(cluster, md, w, reinterpret_cast<df64 *>(sm),
+                                   reinterpret_cast<df64(*)[kClWarps]>(nrmw),
+                                   reinterpret_cast<df64(*)[kClWarps]>(kpw), reinterpret_cast<df64 *>(scal));
+    else if (w.prec[m])
       tridiag_cluster_onchip<double>(cluster, md, w, sm, nrmw, kpw, scal);
     else
       tridiag_cluster_onchip<float>(cluster, md, w, reinterpret_cast<float *>(sm),
@@ -2001,15 +2090,16 @@ void launch_tridiag_smem(const DevPlan &pl, const Work &w, cudaStream_t s, bool 
 // Cluster tridiagonalisation for the molecules listed in mol_list (device).
 // Returns the number of launches.
 int launch_tridiag_cluster(const DevPlan &pl, const Work &w, const int32_t *mol_list, int count, int maxn,
-                           cudaStream_t s, bool tail) {
+                           cudaStream_t s, bool tail, bool split64) {
   if (count <= 0) return 0;
   // two size classes of shared memory (kOnchipSmallBytes)
   const size_t need = onchip_smem_bytes<double>(min(maxn, kClusterBlockedMinN));
   const size_t small = need < kOnchipSmallBytes ? need : kOnchipSmallBytes;
-  k_tridiag_cluster<<<count * kClusterSize, kTrdClThreads, small, s>>>(pl, w, mol_list, tail ? 1 : 0, 0);
+  const int t = tail ? 1 : 0, sp = split64 ? 1 : 0;
+  k_tridiag_cluster<<<count * kClusterSize, kTrdClThreads, small, s>>>(pl, w, mol_list, t, 0, sp);
   int launches = 1;
   if (need > kOnchipSmallBytes) {
-    k_tridiag_cluster<<<count * kClusterSize, kTrdClThreads, need, s>>>(pl, w, mol_list, tail ? 1 : 0, 1);
+    k_tridiag_cluster<<<count * kClusterSize, kTrdClThreads, need, s>>>(pl, w, mol_list, t, 1, sp);
     ++launches;
   }
   if (maxn <= kClusterBlockedMinN) return launches;
