@@ -1720,7 +1720,9 @@ constexpr int kInvitThreads = 256;
 // One thread per eigenvector: LU factorisation with partial pivoting of
 // T - lambda I (factors kept in global scratch, interleaved over eigenvectors
 // so that the sequential sweeps of neighbouring threads are coalesced) and
-// one inverse-iteration solve.
+// one inverse-iteration solve.  U1 holds the reciprocals of the pivots, so
+// that each element costs one division in the factorisation and none in the
+// two solves (a division is ~10 FP64 instructions).
 template <typename T>
 __device__ __forceinline__ void invit_factor(int n, int i, T lam, const T *d, const T *e, T pert, T *U1,
                                              T *U2, T *U3, T *LM, T *PV) {
@@ -1732,8 +1734,10 @@ __device__ __forceinline__ void invit_factor(int n, int i, T lam, const T *d, co
     const T sup2 = (j + 1 < n - 1) ? e[j + 1] : T(0);
     const int64_t o = (int64_t)j * n + i;
     if (fabs(u1) >= fabs(sub)) {
-      const T mult = (u1 != T(0)) ? sub / u1 : T(0);
-      U1[o] = (fabs(u1) < pert) ? ((u1 < T(0)) ? -pert : pert) : u1;
+      const bool tiny = fabs(u1) < pert;
+      const T rinv = T(1) / (tiny ? ((u1 < T(0)) ? -pert : pert) : u1);
+      const T mult = (u1 == T(0)) ? T(0) : (tiny ? sub / u1 : sub * rinv);
+      U1[o] = rinv;
       U2[o] = u2n;
       U3[o] = T(0);
       LM[o] = mult;
@@ -1741,8 +1745,9 @@ __device__ __forceinline__ void invit_factor(int n, int i, T lam, const T *d, co
       u1 = dn - mult * u2n;
       u2n = sup2;
     } else {
-      const T mult = u1 / sub;
-      U1[o] = sub;
+      const T rinv = T(1) / sub;
+      const T mult = u1 * rinv;
+      U1[o] = rinv;
       U2[o] = dn;
       U3[o] = sup2;
       LM[o] = mult;
@@ -1752,7 +1757,7 @@ __device__ __forceinline__ void invit_factor(int n, int i, T lam, const T *d, co
     }
   }
   const int64_t o = (int64_t)(n - 1) * n + i;
-  U1[o] = (fabs(u1) < pert) ? ((u1 < T(0)) ? -pert : pert) : u1;
+  U1[o] = T(1) / ((fabs(u1) < pert) ? ((u1 < T(0)) ? -pert : pert) : u1);
   U2[o] = T(0);
   U3[o] = T(0);
 }
@@ -1813,7 +1818,7 @@ __device__ __forceinline__ void invit_solve(int n, int i, const T *U1, const T *
     for (int c = 0; c < kChunk; ++c) {
       const int j = j0 - c;
       if (j >= 0) {
-        const T sv = (yv[c] - u2[c] * x1 - u3[c] * x2) / u1[c];
+        const T sv = (yv[c] - u2[c] * x1 - u3[c] * x2) * u1[c];
         Y[(int64_t)j * n + i] = sv;
         x2 = x1;
         x1 = sv;
@@ -2005,17 +2010,23 @@ __device__ __forceinline__ void backtransform_column(const MolDesc &md, const Wo
     const T tk = (T)tau[k];
     if (tk == T(0)) continue;
     const T *v = A + (int64_t)k * n;  // reflector k: v[r] = A[k][r] multiplies row r > k
+    // slots below q0 hold only rows r <= k, where v is zero: skipped (a
+    // warp-uniform branch), which halves the FP64 work on average
+    const int q0 = (k + 1) >> 5;
     T vq[NQ];
     T dot = T(0);
 #pragma unroll
     for (int q = 0; q < NQ; ++q) {
-      const int r = lane + 32 * q;
-      vq[q] = (r > k && r < n) ? v[r] : T(0);
-      dot += vq[q] * y[q];
+      if (q >= q0) {
+        const int r = lane + 32 * q;
+        vq[q] = (r > k && r < n) ? v[r] : T(0);
+        dot += vq[q] * y[q];
+      }
     }
     dot = warp_sum(dot) * tk;
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) y[q] -= dot * vq[q];
+    for (int q = 0; q < NQ; ++q)
+      if (q >= q0) y[q] -= dot * vq[q];
   }
 #pragma unroll
   for (int q = 0; q < NQ; ++q) {
