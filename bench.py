@@ -345,12 +345,19 @@ def run_large(args, rank: int, world: int, local: int) -> None:
 
     warnings.simplefilter("ignore")
     if args.large_atoms:
-        # single grown molecules of the given atom counts (seed 7000 + atoms)
-        mols = [molgen.grow(int(a), 7000 + int(a)) for a in args.large_atoms.split(",")]
+        # grown molecules of the given atom counts: "N" one molecule (seed
+        # 7000 + N), "NxK" K molecules of N atoms (seeds 7000 + N + 100000 i)
+        mols = []
+        for item in args.large_atoms.split(","):
+            a, _, k = item.partition("x")
+            mols += [molgen.grow(int(a), 7000 + int(a) + 100000 * i) for i in range(int(k or 1))]
     else:
         mols = molgen.c5_large(16)[: args.large]
     num, pos = pad(mols)
-    calc = GFN1Calculator(torch.as_tensor(num), opts={**OPTS, "profile": True})
+    opts = {**OPTS, "profile": True, "mixed_precision": not args.fp64_only, "fp64_tridiag": args.fp64_tridiag}
+    if args.maxiter:
+        opts["maxiter"] = args.maxiter
+    calc = GFN1Calculator(torch.as_tensor(num), opts=opts)
     p = torch.tensor(pos, device="cuda")
     with ClockSampler(local) as clk:
         torch.cuda.synchronize()
@@ -363,7 +370,8 @@ def run_large(args, rank: int, world: int, local: int) -> None:
         "metric": METRIC, "value": len(mols) / dt, "unit": UNIT, "n_gpus": world, "steps": 1, "warmup": 0,
         "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded CHNO molecules)",
-        "config": {"workload": (f"grown molecules of {args.large_atoms} atoms" if args.large_atoms else
+        "config": {"workload": (f"grown molecules of {args.large_atoms} atoms (NxK: K molecules of N)"
+                                if args.large_atoms else
                                 f"{len(mols)} of the 16 large molecules, 1000-2000 atoms")
                                + ", energy + forces, SCF |dv|<1e-10, one call",
                    "atoms": [int(len(a)) for a, _ in mols],
@@ -484,6 +492,9 @@ def main() -> None:
                     help="batch: 512 x 10-120 atoms (the headline); forces: 256 x 30-60 atoms, perturbed; "
                          "single: one 20-atom molecule per call")
     ap.add_argument("--fp64-only", action="store_true", help="disable the FP32 SCF passes")
+    ap.add_argument("--fp64-tridiag", default="auto", choices=["auto", "native", "df64"],
+                    help="arithmetic of the FP64 passes of the on-chip cluster tridiagonalisation")
+    ap.add_argument("--maxiter", type=int, default=0, help="large-molecule mode: SCF iteration limit (0: 300)")
     ap.add_argument("--no-replay", action="store_true",
                     help="skip the extra call with the reference's mixer (parity_reference_mixer)")
     ap.add_argument("--serve", action="store_true",
@@ -557,7 +568,7 @@ def main() -> None:
     from dxtb_gb300 import GFN1Calculator, _lib
 
     num, pos = pad(mols)
-    run_opts = {**OPTS, "mixed_precision": not args.fp64_only}
+    run_opts = {**OPTS, "mixed_precision": not args.fp64_only, "fp64_tridiag": args.fp64_tridiag}
     # the timed calls replay each SCF pass as a CUDA graph; one extra call
     # with per-class CUDA-event timing gives the stage breakdown
     calc = GFN1Calculator(torch.as_tensor(num), opts=run_opts)

@@ -75,7 +75,7 @@ class Options(C.Structure):
         ("damp_dynamic_factor", C.c_double),
         ("fermi_thresh", C.c_double),
         ("restart_at", C.c_int32),
-        ("reserved", C.c_int32),
+        ("fp64_split", C.c_int32),
     ]
 
 

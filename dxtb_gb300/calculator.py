@@ -75,6 +75,10 @@ DEFAULT_OPTS = {
     "verbosity": 0,
     "profile": False,        # per-stage device timings (last_profile)
     "mixed_precision": True,  # FP32 linear algebra in the early SCF passes
+    # FP64 passes of the on-chip cluster tridiagonalisation: "auto" (double-
+    # float pairs on the FP32 pipe with mixed_precision, native FP64
+    # without), "native" or "df64"
+    "fp64_tridiag": "auto",
     "autotune": "auto",      # tune eigensolver launch shapes on the first call (auto: batches of >= 32)
 }
 # Options of the reference that do not change the numbers this engine
@@ -85,6 +89,7 @@ DEFAULT_OPTS = {
 _ACCEPTED_IGNORED = {"scf_mode", "int_driver", "int_level", "batch_mode", "cache_enabled", "timer",
                      "strict", "log_level"}
 _SCP_MODES = {"potential"}
+_FP64_TRIDIAG = {"auto": 0, "native": 1, "df64": 2}
 
 
 @dataclass
@@ -224,7 +229,8 @@ def _register_fakes() -> None:
 def _pack_options(o: _lib.Options) -> tuple[list[int], list[float]]:
     """The option vectors of ``gbxtb::singlepoint`` (order in torch_ops.cpp)."""
     iopts = [o.maxiter, o.fermi_maxiter, o.broyden_memory, o.want_forces, o.profile, o.mixed_precision,
-             o.mixer, o.generations, o.soft_start, o.mix_guess, o.damp_dynamic, o.no_halogen, o.restart_at]
+             o.mixer, o.generations, o.soft_start, o.mix_guess, o.damp_dynamic, o.no_halogen, o.restart_at,
+             o.fp64_split]
     fopts = [o.x_atol, o.x_atol_max, o.kt, o.broyden_alpha, o.damp, o.damp_init, o.diagonal_offset,
              o.damp_dynamic_factor, o.fermi_thresh]
     return [int(x) for x in iopts], [float(x) for x in fopts]
@@ -288,6 +294,8 @@ def resolve_opts(opts: dict | None) -> dict:
         raise ValueError("broyden_memory must be in 1..29")
     if int(o["anderson_restart"]) < 0:
         raise ValueError("anderson_restart must be >= 0")
+    if str(o["fp64_tridiag"]).lower() not in _FP64_TRIDIAG:
+        raise ValueError(f"fp64_tridiag must be one of {sorted(_FP64_TRIDIAG)}")
     return o
 
 
@@ -317,6 +325,7 @@ def engine_options(o: dict, forces: bool) -> _lib.Options:
     opt.fermi_thresh = 0.0 if o["fermi_thresh"] is None else float(o["fermi_thresh"])
     opt.no_halogen = 1 if "hal" in o["exclude"] else 0
     opt.restart_at = int(o["anderson_restart"])
+    opt.fp64_split = _FP64_TRIDIAG[str(o["fp64_tridiag"]).lower()]
     return opt
 
 

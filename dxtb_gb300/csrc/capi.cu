@@ -116,6 +116,7 @@ int check_options(const gbxtb_options *o) {
   }
   if (!std::isfinite(o->fermi_thresh)) return fail(GBXTB_ERR_ARG, "fermi_thresh must be finite");
   if (o->restart_at < 0) return fail(GBXTB_ERR_ARG, "restart_at must be >= 0");
+  if (o->fp64_split < 0 || o->fp64_split > 2) return fail(GBXTB_ERR_ARG, "fp64_split must be 0, 1 or 2");
   if (o->restart_at > 0 && (o->generations < 1 || o->generations > kHistMax - 1 || !std::isfinite(o->damp) ||
                             !std::isfinite(o->damp_init) || !std::isfinite(o->diagonal_offset)))
     return fail(GBXTB_ERR_ARG, "restart_at needs valid Anderson options (generations, damp, damp_init, offset)");
@@ -534,12 +535,12 @@ int enqueue_pass(gbxtb_plan *plan, const Work &w, const gbxtb_options &o, bool t
   if (opts->mixed_precision) launch_tridiag_smem(pl, w, s, tail);
   int ntrd = opts->mixed_precision ? plan->smem_launches : 0;
   if (tail) {
-    ntrd += launch_tridiag_cluster(pl, w, w.active_list, active, plan->maxn, s, true, opts->mixed_precision != 0);
+    ntrd += launch_tridiag_cluster(pl, w, w.active_list, active, plan->maxn, s, true, split64(*opts));
   } else {
     // large FP64 passes and FP32 passes too large for shared memory on 8-SM
     // clusters, the rest one CTA per molecule
     if (nclus > 0)
-      ntrd += launch_tridiag_cluster(pl, w, w.cluster_list, nclus, plan->maxn, s, false, opts->mixed_precision != 0);
+      ntrd += launch_tridiag_cluster(pl, w, w.cluster_list, nclus, plan->maxn, s, false, split64(*opts));
     launch_tridiag(pl, w, plan->maxn, s);
     ntrd += 1;
   }

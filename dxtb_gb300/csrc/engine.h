@@ -16,10 +16,10 @@ void launch_lowp_copies(const DevPlan &pl, const Work &w, cudaStream_t s);
 // tail: the launch shapes of the tail of a batch (FP32 passes above
 // kTailClusterMinN AOs move from k_tridiag_smem to the cluster kernel)
 void launch_tridiag_smem(const DevPlan &pl, const Work &w, cudaStream_t s, bool tail = false);
-// split64: FP64 passes of the on-chip kernel in double-float arithmetic
+// df64_passes: FP64 passes of the on-chip kernel in double-float arithmetic
 // (df64.cuh) on the FP32 pipe
 int launch_tridiag_cluster(const DevPlan &pl, const Work &w, const int32_t *mol_list, int count, int maxn,
-                           cudaStream_t s, bool tail = false, bool split64 = false);
+                           cudaStream_t s, bool tail = false, bool df64_passes = false);
 void launch_bisect(const DevPlan &pl, const Work &w, int maxn, double kt, const int32_t *mol_list, int count,
                    int threads, cudaStream_t s);
 void launch_invit(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s);

@@ -53,6 +53,12 @@ __host__ __device__ __forceinline__ bool cluster_pass(int prec, int nao) {
   return prec ? nao > kClusterMinN : nao > kSmemTridiagMaxN;
 }
 
+// FP64 passes of the on-chip cluster tridiagonalisation in double-float
+// arithmetic (gbxtb_options.fp64_split)
+inline bool split64(const gbxtb_options &o) {
+  return o.fp64_split == 2 || (o.fp64_split == 0 && o.mixed_precision != 0);
+}
+
 // molecule phases of the SCF state machine
 constexpr int kPhaseIterate = 0;  // mixing iterations
 constexpr int kPhaseFinal = 1;    // one more V -> Q pass with the unmixed potential

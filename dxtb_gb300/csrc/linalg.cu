@@ -1048,7 +1048,7 @@ __host__ __device__ constexpr size_t onchip_smem_bytes(int n) {
 constexpr size_t kOnchipSmallBytes = 110 * 1024;
 
 __global__ void __cluster_dims__(kClusterSize, 1, 1) __launch_bounds__(kTrdClThreads)
-    k_tridiag_cluster(DevPlan pl, Work w, const int32_t *mol_list, int tail, int big, int split64) {
+    k_tridiag_cluster(DevPlan pl, Work w, const int32_t *mol_list, int tail, int big, int df64_passes) {
   cg::cluster_group cluster = cg::this_cluster();
   const int m = list_mol(w, mol_list, blockIdx.x / kClusterSize);
   if (m < 0) return;  // the whole cluster
@@ -1065,7 +1065,7 @@ __global__ void __cluster_dims__(kClusterSize, 1, 1) __launch_bounds__(kTrdClThr
   const bool other_launch = big ? need <= kOnchipSmallBytes : need > kOnchipSmallBytes;
   const bool done = (w.phase[m] == kPhaseDone) || smem32 || md.nao > kClusterBlockedMinN || other_launch;
   if (!done) {
-    if (w.prec[m] && split64)
+    if (w.prec[m] && df64_passes)
       tridiag_cluster_onchip<df64>(cluster, md, w, reinterpret_cast<df64 *>(sm),
                                    reinterpret_cast<df64(*)[kClWarps]>(nrmw),
                                    reinterpret_cast<df64(*)[kClWarps]>(kpw), reinterpret_cast<df64 *>(scal));
@@ -1993,6 +1993,41 @@ __global__ void __launch_bounds__(kBtThreads) k_backtransform(DevPlan pl, Work w
 // registers (row r in lane r % 32, slot r / 32), so applying a reflector is a
 // warp reduction and a register update, with no CTA barrier; the reflector
 // rows are read through L1, shared by the eight warps of a CTA.
+// Reflector k is zero in rows r <= k, so slots below (k + 1) / 32 take no
+// part: the reflectors are applied in ranges of 32 with the first slot QS a
+// compile-time constant (every load of a reflector still in flight at once),
+// which halves the FP64 work on average.
+template <typename T, int NQ, int QS>
+__device__ __forceinline__ void bt_apply_range(T (&y)[NQ], const T *A, const double *tau, int n, int lane,
+                                               int khi, int klo) {
+  for (int k = khi; k >= klo; --k) {
+    const T tk = (T)tau[k];
+    if (tk == T(0)) continue;
+    const T *v = A + (int64_t)k * n;  // reflector k: v[r] = A[k][r] multiplies row r > k
+    T vq[NQ - QS];
+    T dot = T(0);
+#pragma unroll
+    for (int q = QS; q < NQ; ++q) {
+      const int r = lane + 32 * q;
+      vq[q - QS] = (r > k && r < n) ? v[r] : T(0);
+      dot += vq[q - QS] * y[q];
+    }
+    dot = warp_sum(dot) * tk;
+#pragma unroll
+    for (int q = QS; q < NQ; ++q) y[q] -= dot * vq[q - QS];
+  }
+}
+
+// reflectors kstart, kstart - 1, ..., 0 in the ranges (k + 1) / 32 = QS, QS - 1, ..., 0
+template <typename T, int NQ, int QS>
+__device__ __forceinline__ void bt_apply_from(T (&y)[NQ], const T *A, const double *tau, int n, int lane,
+                                              int kstart) {
+  const int klo = 32 * QS - 1 > 0 ? 32 * QS - 1 : 0;
+  const int khi = kstart < 32 * QS + 30 ? kstart : 32 * QS + 30;
+  if (khi >= klo) bt_apply_range<T, NQ, QS>(y, A, tau, n, lane, khi, klo);
+  if constexpr (QS > 0) bt_apply_from<T, NQ, QS - 1>(y, A, tau, n, lane, kstart);
+}
+
 template <typename T, int NQ>
 __device__ __forceinline__ void backtransform_column(const MolDesc &md, const Work &w, int c) {
   const int n = md.nao;
@@ -2006,28 +2041,7 @@ __device__ __forceinline__ void backtransform_column(const MolDesc &md, const Wo
     const int r = lane + 32 * q;
     y[q] = (r < n) ? Y[(int64_t)r * n + c] : T(0);
   }
-  for (int k = n - 3; k >= 0; --k) {
-    const T tk = (T)tau[k];
-    if (tk == T(0)) continue;
-    const T *v = A + (int64_t)k * n;  // reflector k: v[r] = A[k][r] multiplies row r > k
-    // slots below q0 hold only rows r <= k, where v is zero: skipped (a
-    // warp-uniform branch), which halves the FP64 work on average
-    const int q0 = (k + 1) >> 5;
-    T vq[NQ];
-    T dot = T(0);
-#pragma unroll
-    for (int q = 0; q < NQ; ++q) {
-      if (q >= q0) {
-        const int r = lane + 32 * q;
-        vq[q] = (r > k && r < n) ? v[r] : T(0);
-        dot += vq[q] * y[q];
-      }
-    }
-    dot = warp_sum(dot) * tk;
-#pragma unroll
-    for (int q = 0; q < NQ; ++q)
-      if (q >= q0) y[q] -= dot * vq[q];
-  }
+  bt_apply_from<T, NQ, NQ - 1>(y, A, tau, n, lane, n - 3);
 #pragma unroll
   for (int q = 0; q < NQ; ++q) {
     const int r = lane + 32 * q;
@@ -2038,7 +2052,7 @@ __device__ __forceinline__ void backtransform_column(const MolDesc &md, const Wo
 // grid (column groups of 8, molecules): molecule mol_list[y] (all if null);
 // every molecule has at most 32 * NQ AOs
 template <int NQ>
-__global__ void __launch_bounds__(256) k_backtransform_warp(DevPlan pl, Work w, const int32_t *mol_list) {
+__global__ void __launch_bounds__(256, 2) k_backtransform_warp(DevPlan pl, Work w, const int32_t *mol_list) {
   const int m = mol_list ? list_mol(w, mol_list, blockIdx.y) : (int)blockIdx.y;
   if (m < 0) return;
   if (w.phase[m] == kPhaseDone) return;
@@ -2101,12 +2115,12 @@ void launch_tridiag_smem(const DevPlan &pl, const Work &w, cudaStream_t s, bool 
 // Cluster tridiagonalisation for the molecules listed in mol_list (device).
 // Returns the number of launches.
 int launch_tridiag_cluster(const DevPlan &pl, const Work &w, const int32_t *mol_list, int count, int maxn,
-                           cudaStream_t s, bool tail, bool split64) {
+                           cudaStream_t s, bool tail, bool df64_passes) {
   if (count <= 0) return 0;
   // two size classes of shared memory (kOnchipSmallBytes)
   const size_t need = onchip_smem_bytes<double>(min(maxn, kClusterBlockedMinN));
   const size_t small = need < kOnchipSmallBytes ? need : kOnchipSmallBytes;
-  const int t = tail ? 1 : 0, sp = split64 ? 1 : 0;
+  const int t = tail ? 1 : 0, sp = df64_passes ? 1 : 0;
   k_tridiag_cluster<<<count * kClusterSize, kTrdClThreads, small, s>>>(pl, w, mol_list, t, 0, sp);
   int launches = 1;
   if (need > kOnchipSmallBytes) {

@@ -462,11 +462,11 @@ int gbxtb_pool_step_launch(gbxtb_pool *pool, void *stream) {
     launch_gemm(pl, w, plan->tile0, plan->ntile, 6, 0, s);
     if (o.mixed_precision) launch_tridiag_smem(pl, w, s, tail);
     if (tail) {
-      launch_tridiag_cluster(pl, w, w.active_list, active, plan->maxn, s, true, o.mixed_precision != 0);
+      launch_tridiag_cluster(pl, w, w.active_list, active, plan->maxn, s, true, split64(o));
       launch_bisect(pl, w, plan->maxn, o.kt, w.active_list, active, 32, s);
     } else {
       if (nclus > 0)
-        launch_tridiag_cluster(pl, w, w.cluster_list, nclus, plan->maxn, s, false, o.mixed_precision != 0);
+        launch_tridiag_cluster(pl, w, w.cluster_list, nclus, plan->maxn, s, false, split64(o));
       launch_tridiag(pl, w, plan->maxn, s);
       launch_bisect(pl, w, plan->maxn, o.kt, nullptr, pl.nmol, 256, s);
     }

@@ -23,7 +23,7 @@
 //
 // iopts: maxiter, fermi_maxiter, broyden_memory, want_forces, profile,
 //        mixed_precision, mixer, generations, soft_start, mix_guess,
-//        damp_dynamic, no_halogen, restart_at
+//        damp_dynamic, no_halogen, restart_at, fp64_split
 // fopts: x_atol, x_atol_max, kt, broyden_alpha, damp, damp_init,
 //        diagonal_offset, damp_dynamic_factor, fermi_thresh
 #include <ATen/ATen.h>
@@ -38,7 +38,7 @@
 
 namespace {
 
-constexpr size_t kIopts = 13, kFopts = 9;
+constexpr size_t kIopts = 14, kFopts = 9;
 
 gbxtb_options unpack_options(const std::vector<int64_t> &io, const std::vector<double> &fo) {
   TORCH_CHECK(io.size() == kIopts, "gbxtb::singlepoint: iopts needs ", kIopts, " entries, got ", io.size());
@@ -58,6 +58,7 @@ gbxtb_options unpack_options(const std::vector<int64_t> &io, const std::vector<d
   o.damp_dynamic = (int32_t)io[10];
   o.no_halogen = (int32_t)io[11];
   o.restart_at = (int32_t)io[12];
+  o.fp64_split = (int32_t)io[13];
   o.x_atol = fo[0];
   o.x_atol_max = fo[1];
   o.kt = fo[2];

@@ -138,7 +138,11 @@ typedef struct {
                               maxiter budget, so that it follows the reference's
                               own SCF where the faster mixer does not converge;
                               0: never */
-  int32_t reserved;        /* 0 */
+  int32_t fp64_split;      /* arithmetic of the FP64 passes of the on-chip cluster
+                              tridiagonalisation (molecules of kClusterMinN < n
+                              <= 400 AOs): 0 (auto): double-float pairs on the
+                              FP32 pipe (~48 bits) with mixed_precision, native
+                              FP64 without; 1: native FP64; 2: double-float */
 } gbxtb_options;
 
 /* The reference's default SCF options (calculators/config/scf.py:139-190,

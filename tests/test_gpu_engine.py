@@ -352,6 +352,23 @@ def test_mixed_precision_same_fixed_point():
         assert np.abs(g64[off[k]:off[k + 1]] - g32[off[k]:off[k + 1]]).max() < 1e-8
 
 
+def test_df64_tridiagonalisation_same_fixed_point():
+    """FP64 passes with the on-chip cluster tridiagonalisation in double-float
+    arithmetic (~48 bits) end on the fixed point of native FP64: every pass
+    in FP64, molecules of 150-330 AOs (all on the cluster kernel), energies
+    within 1e-10 Eh, forces 1e-8 Eh/bohr, and the same SCF pass counts up to
+    one."""
+    mols = [molgen.grow(a, 8100 + a) for a in (50, 70, 90, 110)]
+    num, pos = pad(mols)
+    p = torch.tensor(pos, device="cuda")
+    rn = calc_for(num, mixed_precision=False, fp64_tridiag="native").singlepoint(p, forces=True)
+    rd = calc_for(num, mixed_precision=False, fp64_tridiag="df64").singlepoint(p, forces=True)
+    assert (rn.status == 0).all() and (rd.status == 0).all()
+    assert np.abs(rn.energy.cpu().numpy() - rd.energy.cpu().numpy()).max() < 1e-10
+    assert np.abs(rn.gradient.cpu().numpy() - rd.gradient.cpu().numpy()).max() < 1e-8
+    assert np.abs(rn.iterations - rd.iterations).max() <= 1
+
+
 def test_large_molecule_against_oracle():
     """A 300-atom molecule (~900 AOs): the block-wise Cholesky over the whole
     GPU, the global-memory lead-in of the on-chip FP32 tridiagonalisation

@@ -37,6 +37,7 @@ def test_mixer_options_reach_the_engine():
     ({"exclude": []}, ValueError),
     ({"exclude": ["disp", "es3"]}, NotImplementedError),
     ({"exclude": ["disp", "rep"]}, NotImplementedError),
+    ({"fp64_tridiag": "quad"}, ValueError),
 ])
 def test_unsupported_options_raise(opts, err):
     with pytest.raises(err):
@@ -54,3 +55,11 @@ def test_halogen_bond_switch():
     assert engine_options(resolve_opts({"exclude": ["disp", "hal"]}), False).no_halogen == 1
     # GFN2-only terms are absent from GFN1 anyway
     assert engine_options(resolve_opts({"exclude": ["disp", "aes2", "d4sc"]}), False).no_halogen == 0
+
+
+def test_fp64_tridiag_switch():
+    """The arithmetic of the FP64 on-chip tridiagonalisation reaches the C
+    options (0 auto, 1 native FP64, 2 double-float)."""
+    assert engine_options(resolve_opts(BASE), False).fp64_split == 0
+    assert engine_options(resolve_opts({**BASE, "fp64_tridiag": "native"}), False).fp64_split == 1
+    assert engine_options(resolve_opts({**BASE, "fp64_tridiag": "df64"}), False).fp64_split == 2
