@@ -36,6 +36,9 @@ METRIC = "single-points+forces/s (fp64, |dE|<=1e-8 Eh) batched vs plain on GB300
 UNIT = "molecules/s"
 NMOL = 512
 OPTS = {"exclude": ["disp"], "maxiter": 300, "x_atol": 1e-10, "x_atol_max": 1e-10}
+# DRAM read + write bytes of the k_tridiag* kernels in one call on the
+# 512-molecule workload (ncu capture, dram__bytes_read.sum + dram__bytes_write.sum)
+TRIDIAG_DRAM_BYTES_512 = 8.54e9
 CPU_SAMPLE = 48           # molecules in the host-core baseline sample
 REF_STEP_SAMPLE = 24      # molecules per step of the reference arm
 PLAIN_SAMPLE = 24         # molecules timed one call each (the plain per-molecule GPU path)
@@ -690,6 +693,14 @@ def main() -> None:
             "peak_source": "measured FP64 FMA microbenchmark (gbxtb_fp64_peak) in this run; "
                            "MEASURED_PEAKS.json holds no FP64 figure",
             "fp64_mma_tflops": g.value / 1e3}
+    if dominant == "tridiag" and nmol == NMOL and args.workload == "batch" and world == 1:
+        # DRAM bytes of the tridiagonalisation kernels per 512-molecule call,
+        # one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum over
+        # the k_tridiag* launches of a call)
+        roof["traffic"] = TRIDIAG_DRAM_BYTES_512
+        roof["traffic_note"] = ("bytes per step (one 512-molecule call) of the tridiagonalisation kernels, "
+                                "from one ncu capture of this workload; ~ the algorithmic bytes (each pass reads "
+                                "the matrix once and writes its reflectors)")
     if dominant in fl and per_step_ms[dominant] > 0:
         f64, f32 = fl[dominant]
         achieved = (f64 + f32 / FP32_PER_FP64) / (per_step_ms[dominant] * 1e-3) / 1e12
