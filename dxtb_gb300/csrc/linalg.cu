@@ -41,6 +41,7 @@
 #include <algorithm>
 #include <cooperative_groups.h>
 #include <mutex>
+#include <type_traits>
 
 namespace cg = cooperative_groups;
 
@@ -887,55 +888,47 @@ __device__ __forceinline__ void tridiag_cluster_onchip(cg::cluster_group &cluste
   using O = ClOps<T>;
   using G = typename O::G;
   using Acc = typename O::Acc;
+  // FP32: every warp forms the scalars it needs itself (no CTA barrier);
+  // FP64 and double-float: warp 0 alone (the FP64 pipe is scarce)
+  constexpr bool kOneWarp = !std::is_same<T, float>::value;
   const int rank = (int)cluster.block_rank();
   const int n = md.nao;
   const int nloc = (n - rank + kClusterSize - 1) / kClusterSize;  // rows rank, rank + 8, ...
   G *Ag = mat_view<G>(w.A, md.mat0);
   double *d = w.d + md.ao0, *e = w.e + md.ao0, *tau = w.tau + md.ao0;
-  T *rows = sm;                                   // [nloc_max][n]
   const int nloc_max = (n + kClusterSize - 1) / kClusterSize;
-  T *vs = rows + (size_t)nloc_max * n;            // [n] reflector
-  T *wv = vs + n;                                 // [n] w of all rows
-  T *ps = wv + n;                                 // [nloc_max] p of own rows (read by all)
+  T *rows = sm;                                   // [nloc_max][n]
+  T *vsb = rows + (size_t)nloc_max * n;           // [2][n] reflector v_k by row k+1+t, by parity of k
+  T *wv = vsb + 2 * (size_t)n;                    // [n] w_k by row k+1+t
+  T *psb = wv + n;                                // [2][nloc_max] p_k of own rows (read by all)
+  T *colb = psb + 2 * (size_t)nloc_max;           // [2][nloc_max] column k+1 of own rows before step k's update
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  // element (i, j) of the matrix in its owner's shared memory
-  auto remote = [&](int i, int j) -> T {
-    const T *base = cluster.map_shared_rank(rows, i % kClusterSize);
-    return base[(size_t)(i / kClusterSize) * n + j];
+  auto own = [&](int i, int j) -> T & { return rows[(size_t)(i / kClusterSize) * n + j]; };
+  // first own local row index with row >= r
+  auto first_local = [&](int r) {
+    const int f = (r - rank + kClusterSize - 1) / kClusterSize;
+    return f > 0 ? f : 0;
   };
-  // per-warp partial norm of column c over own rows i >= c + 2, published in buffer b
-  auto publish_norm = [&](int c, int b, int lfirst) {
-    Acc part = O::acc0();
-    for (int li = lfirst + lane + 32 * wid; li < nloc; li += 32 * nw) {
-      const int i = rank + li * kClusterSize;
-      if (i >= c + 2) {
-        const T x = rows[(size_t)li * n + c];
-        O::dot(part, x, x);
-      }
-    }
-    const T sum = cl_warp_sum(O::fin(part));
-    if (lane == 0) nrmw[b][wid] = sum;
-  };
-  // load own rows
-  for (int li = wid; li < nloc; li += nw) {
-    const G *src = Ag + (int64_t)(rank + li * kClusterSize) * n;
-    T *dst = rows + (size_t)li * n;
-    for (int j = lane; j < n; j += 32) dst[j] = O::load(src[j]);
-  }
-  __syncthreads();
-  publish_norm(0, 0, 0);
-  cluster.sync();
-  for (int k = 0; k + 2 < n; ++k) {
+  // Reflector k from X[0..m1) = column k of rows k+1..n-1 (identical in every
+  // CTA): squared norm of X[1..) by a fixed-order block reduction, scalars,
+  // then X becomes v_k in place (v_k[0] = 1).  Without reflection (zero
+  // norm) tau_k = 0 and v_k = e_1: the step's update is then exactly the
+  // identity, so the step keeps the same barriers.
+  auto make_reflector = [&](int k, T *X) -> T {
     const int m1 = n - k - 1;
-    const int buf = k & 1;
-    // (a) reflector scalars, by warp 0
-    if (wid == 0) {
-      const T xn2 = cluster_partial_sum(cluster, nrmw, buf);
-      const T alpha = remote(k + 1, k);
-      T tk, scale;
+    const T alpha = X[0];  // read by every thread before the barrier below, X[0] is rewritten after it
+    Acc part = O::acc0();
+    for (int t = 1 + threadIdx.x; t < m1; t += blockDim.x) O::dot(part, X[t], X[t]);
+    const T ws = cl_warp_sum(O::fin(part));
+    if (lane == 0) nrmw[0][wid] = ws;
+    __syncthreads();
+    T tk = O::zero(), scale = O::zero();
+    if (!kOneWarp || wid == 0) {
+      T xn2 = O::zero();
+      for (int q = 0; q < kClWarps; ++q) xn2 = O::add(xn2, nrmw[0][q]);
       double beta;
       O::reflector(xn2, alpha, tk, scale, beta);
-      if (lane == 0) {
+      if (threadIdx.x == 0) {
         scal[0] = tk;
         scal[1] = scale;
         if (rank == 0) {
@@ -943,29 +936,60 @@ __device__ __forceinline__ void tridiag_cluster_onchip(cg::cluster_group &cluste
           tau[k] = O::to_d(tk);
         }
       }
-    } else if (threadIdx.x == 32 && rank == k % kClusterSize) {
-      d[k] = O::to_d(rows[(size_t)(k / kClusterSize) * n + k]);
     }
-    __syncthreads();
-    const T tk = scal[0], scale = scal[1];
-    // first own row at or after k + 1
-    const int lfirst = (k + 1 - rank + kClusterSize - 1) / kClusterSize > 0
-                           ? (k + 1 - rank + kClusterSize - 1) / kClusterSize : 0;
-    if (O::is_zero(tk)) {
-      // no reflection: publish the partial norm of column k + 1 and go on
-      publish_norm(k + 1, buf ^ 1, lfirst);
-      cluster.sync();
-      continue;
+    if (kOneWarp) {
+      __syncthreads();
+      tk = scal[0];
+      scale = scal[1];
     }
-    for (int t = threadIdx.x; t < m1; t += blockDim.x) vs[t] = (t == 0) ? O::one() : O::mul(remote(k + 1 + t, k), scale);
-    __syncthreads();
+    for (int t = threadIdx.x; t < m1; t += blockDim.x) X[t] = (t == 0) ? O::one() : O::mul(X[t], scale);
+    return tk;
+  };
+  // load own rows
+  for (int li = wid; li < nloc; li += nw) {
+    const G *src = Ag + (int64_t)(rank + li * kClusterSize) * n;
+    T *dst = rows + (size_t)li * n;
+    for (int j = lane; j < n; j += 32) dst[j] = O::load(src[j]);
+  }
+  cluster.sync();
+  if (n < 3) {
+    if (threadIdx.x == 0) {
+      if (n == 2) {
+        if (rank == 0) d[0] = O::to_d(own(0, 0));
+        if (rank == 1) {
+          d[1] = O::to_d(own(1, 1));
+          e[0] = O::to_d(own(1, 0));
+        }
+      } else if (rank == 0) {
+        d[0] = O::to_d(own(0, 0));
+      }
+    }
+    return;
+  }
+  // reflector 0 from column 0, gathered from the owners
+  for (int t = threadIdx.x; t < n - 1; t += blockDim.x) {
+    const int i = 1 + t;
+    vsb[t] = cluster.map_shared_rank(rows, i % kClusterSize)[(size_t)(i / kClusterSize) * n];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && rank == 0) d[0] = O::to_d(own(0, 0));
+  T tk = make_reflector(0, vsb);
+  __syncthreads();
+  for (int k = 0; k + 2 < n; ++k) {
+    const int m1 = n - k - 1;
+    const int buf = k & 1;
+    T *vs = vsb + (size_t)buf * n;
+    T *ps = psb + (size_t)buf * nloc_max;
+    T *colbuf = colb + (size_t)buf * nloc_max;
+    const int lfirst = first_local(k + 1);
     if (rank == 0)
       for (int t = threadIdx.x; t < m1; t += blockDim.x) Ag[(int64_t)k * n + k + 1 + t] = O::store(vs[t]);
-    // (b) p = tau A22 v for own rows, four rows of a warp at a time; per-warp partial p.v
+    if (threadIdx.x == 32 && k > 0 && rank == k % kClusterSize) d[k] = O::to_d(own(k, k));
+    // (1) p_k = tau A22 v for own rows (warp w takes the local rows li = w mod
+    // nw, four at a time; the same rows it updates below), per-warp partial p.v
     Acc pv = O::acc0();
-    for (int l0 = lfirst + wid; l0 < nloc; l0 += 4 * nw) {
-      // rows l0, l0 + nw, l0 + 2 nw, l0 + 3 nw (past the end: row l0 again,
-      // result unused)
+    const int l00 = lfirst + ((wid - lfirst) % nw + nw) % nw;  // first local row >= lfirst with li = wid mod nw
+    for (int l0 = l00; l0 < nloc; l0 += 4 * nw) {
       const int l1 = l0 + nw < nloc ? l0 + nw : l0, l2 = l0 + 2 * nw < nloc ? l0 + 2 * nw : l0,
                 l3 = l0 + 3 * nw < nloc ? l0 + 3 * nw : l0;
       const T *r0 = rows + (size_t)l0 * n + (k + 1), *r1 = rows + (size_t)l1 * n + (k + 1),
@@ -978,7 +1002,6 @@ __device__ __forceinline__ void tridiag_cluster_onchip(cg::cluster_group &cluste
         O::dot(a2, r2[j], vj);
         O::dot(a3, r3[j], vj);
       }
-      // lane 8 q: p of row l0 + q nw
       const T c = O::mul(warp_sum4(O::fin(a0), O::fin(a1), O::fin(a2), O::fin(a3)), tk);
       T pq[4];
 #pragma unroll
@@ -995,42 +1018,57 @@ __device__ __forceinline__ void tridiag_cluster_onchip(cg::cluster_group &cluste
       }
     }
     if (lane == 0) kpw[buf][wid] = O::fin(pv);
+    // (2) column k+1 of own rows k+2.. before this step's update, for every CTA
+    for (int li = first_local(k + 2) + threadIdx.x; li < nloc; li += blockDim.x)
+      colbuf[li] = rows[(size_t)li * n + (k + 1)];
     cluster.sync();
-    // (c) p.v by warp 0, then w for all rows
-    if (wid == 0) {
+    // (3) p.v and w_k for all rows (p gathered from the owners); the
+    // column k+1 copies gathered alongside
+    const bool next = k + 3 < n;  // a reflector k+1 follows
+    T *X = vsb + (size_t)(buf ^ 1) * n;  // column k+1 of rows k+2.., then v_{k+1}
+    T half;
+    if (!kOneWarp || wid == 0) {
       const T K = cluster_partial_sum(cluster, kpw, buf);
-      if (lane == 0) scal[2] = O::half_prod(tk, K);
+      half = O::half_prod(tk, K);
+      if (kOneWarp && lane == 0) scal[2] = half;
     }
-    __syncthreads();
-    const T half = scal[2];
+    if (kOneWarp) {
+      __syncthreads();
+      half = scal[2];
+    }
     for (int t = threadIdx.x; t < m1; t += blockDim.x) {
       const int i = k + 1 + t;
-      const T p = cluster.map_shared_rank(ps, i % kClusterSize)[i / kClusterSize];
+      const int r = i % kClusterSize, li = i / kClusterSize;
+      const T p = cluster.map_shared_rank(psb, r)[(size_t)buf * nloc_max + li];
       wv[t] = O::axpy_neg(p, half, vs[t]);
+      if (next && t >= 1) X[t - 1] = cluster.map_shared_rank(colb, r)[(size_t)buf * nloc_max + li];
     }
     __syncthreads();
-    // (d) rank-2 update of own rows, per-warp partial norm of column k + 1
-    Acc part = O::acc0();
-    for (int li = lfirst + wid; li < nloc; li += nw) {
+    // (4) column k+1 after this step's update, for rows k+2.. (the same
+    // expression the owners evaluate below, so bitwise their values)
+    if (next)
+      for (int t = 1 + threadIdx.x; t < m1; t += blockDim.x)
+        X[t - 1] = O::rank2(X[t - 1], vs[t], wv[0], wv[t], vs[0]);
+    // (5) A22 -= v w^T + w v^T on own rows
+    for (int li = l00; li < nloc; li += nw) {
       const int t = rank + li * kClusterSize - (k + 1);
       T *row = rows + (size_t)li * n + (k + 1);
       const T vi = vs[t], wi = wv[t];
-      for (int j = lane; j < m1; j += 32) {
-        const T a = O::rank2(row[j], vi, wv[j], wi, vs[j]);
-        row[j] = a;
-        if (j == 0 && t >= 2) O::dot(part, a, a);  // column k + 1, rows k + 3 ... (lane 0)
-      }
+      for (int j = lane; j < m1; j += 32) row[j] = O::rank2(row[j], vi, wv[j], wi, vs[j]);
     }
-    if (lane == 0) nrmw[buf ^ 1][wid] = O::fin(part);
-    cluster.sync();
+    // (6) reflector k+1
+    if (next) {
+      __syncthreads();
+      tk = make_reflector(k + 1, X);
+    }
+    __syncthreads();
   }
-  if (rank == 0 && threadIdx.x == 0) {
-    if (n >= 2) {
-      d[n - 2] = O::to_d(remote(n - 2, n - 2));
-      d[n - 1] = O::to_d(remote(n - 1, n - 1));
-      e[n - 2] = O::to_d(remote(n - 1, n - 2));
-    } else {
-      d[0] = O::to_d(remote(0, 0));
+  // the last 2 x 2 block, from the owners' rows after the last update
+  if (threadIdx.x == 0) {
+    if (rank == (n - 2) % kClusterSize) d[n - 2] = O::to_d(own(n - 2, n - 2));
+    if (rank == (n - 1) % kClusterSize) {
+      d[n - 1] = O::to_d(own(n - 1, n - 1));
+      e[n - 2] = O::to_d(own(n - 1, n - 2));
     }
   }
 }
@@ -1038,7 +1076,7 @@ __device__ __forceinline__ void tridiag_cluster_onchip(cg::cluster_group &cluste
 // Shared memory of tridiag_cluster_onchip for n AOs.
 template <typename T>
 __host__ __device__ constexpr size_t onchip_smem_bytes(int n) {
-  return sizeof(T) * ((size_t)((n + kClusterSize - 1) / kClusterSize) * (n + 1) + 2 * (size_t)n);
+  return sizeof(T) * ((size_t)((n + kClusterSize - 1) / kClusterSize) * (n + 4) + 3 * (size_t)n);
 }
 // Molecules whose rows need at most this much shared memory per CTA run in
 // a launch sized for it, which lets two CTAs share an SM (FP64 up to 320

@@ -117,50 +117,63 @@ def test_blocked_model_zero_column():
 
 def onchip_cluster_tridiag(a: np.ndarray, csize: int = 8):
     """Phase-by-phase model of tridiag_cluster_onchip (csrc/linalg.cu): rows
-    owned cyclically by `csize` CTAs in their shared memory, partial column
-    norms published per CTA (the norm of column k+1 accumulated during the
-    update of step k), p of own rows gathered by every CTA.  Returns d, e,
-    tau and the reflector rows, in the kernel's index conventions."""
+    owned cyclically by `csize` CTAs in their shared memory, one exchange per
+    step.  Before it every CTA publishes p_k of its rows, its partial p.v and
+    a copy of column k+1 of its rows as they are before the step's update;
+    after it every CTA forms w_k, applies the update to that copy of column
+    k+1 itself (for all rows) and builds reflector k+1 from it, while the
+    owners update their rows.  Without reflection tau = 0 and v = e_1 (the
+    update is then the identity).  Returns d, e, tau and the reflector rows,
+    in the kernel's index conventions."""
     n = a.shape[0]
     own = [[i for i in range(n) if i % csize == r] for r in range(csize)]
     rows = {i: a[i].copy() for i in range(n)}  # row i on CTA i % csize
     d, e, tau = np.zeros(n), np.zeros(n), np.zeros(n)
     refl = np.zeros((n, n))
-    nrm = [sum(rows[i][0] ** 2 for i in own[r] if i >= 2) for r in range(csize)]
-    for k in range(n - 2):
-        m1 = n - k - 1
-        xn2 = sum(nrm)
-        alpha = rows[k + 1][k]
+
+    def reflector(k, x):
+        """x: column k of rows k+1.. (identical in every CTA) -> tau_k, v_k."""
+        xn2 = float(np.dot(x[1:], x[1:]))
+        alpha = x[0]
         tk, scale, beta = 0.0, 0.0, alpha
         if xn2 != 0.0:
             beta = -np.copysign(np.sqrt(alpha * alpha + xn2), alpha)
             tk = (beta - alpha) / beta
             scale = 1.0 / (alpha - beta)
-        d[k], e[k], tau[k] = rows[k][k], beta, tk
-        if tk == 0.0:
-            nrm = [sum(rows[i][k + 1] ** 2 for i in own[r] if i >= k + 3) for r in range(csize)]
-            continue
-        v = np.array([1.0] + [rows[k + 1 + t][k] * scale for t in range(1, m1)])
+        e[k], tau[k] = beta, tk
+        return tk, np.concatenate([[1.0], x[1:] * scale])
+
+    d[0] = rows[0][0]
+    tk, v = reflector(0, np.array([rows[i][0] for i in range(1, n)]))
+    for k in range(n - 2):
+        m1 = n - k - 1
         refl[k, k + 1:] = v
-        ps, kp = {}, [0.0] * csize
+        if k > 0:
+            d[k] = rows[k][k]
+        # before the exchange: p_k and p.v partials of own rows, column k+1 copies
+        ps, kp, col = {}, [0.0] * csize, {}
         for r in range(csize):
             for i in own[r]:
-                if i < k + 1:
-                    continue
-                t = i - (k + 1)
-                ps[i] = tk * np.dot(rows[i][k + 1:], v)
-                kp[r] += ps[i] * v[t]
+                if i >= k + 1:
+                    ps[i] = tk * np.dot(rows[i][k + 1:], v)
+                    kp[r] += ps[i] * v[i - (k + 1)]
+                if i >= k + 2:
+                    col[i] = rows[i][k + 1]
+        # after it: w_k, the updated column k+1 and reflector k+1 (every CTA)
         half = 0.5 * tk * sum(kp)
         wv = np.array([ps[k + 1 + t] - half * v[t] for t in range(m1)])
-        nrm = [0.0] * csize
+        vnext = None
+        if k + 3 < n:
+            x = np.array([col[i] - v[i - (k + 1)] * wv[0] - wv[i - (k + 1)] * v[0] for i in range(k + 2, n)])
+            tnext, vnext = reflector(k + 1, x)
+        # owners' update
         for r in range(csize):
             for i in own[r]:
-                if i < k + 1:
-                    continue
-                t = i - (k + 1)
-                rows[i][k + 1:] -= v[t] * wv + wv[t] * v
-                if t >= 2:
-                    nrm[r] += rows[i][k + 1] ** 2
+                if i >= k + 1:
+                    t = i - (k + 1)
+                    rows[i][k + 1:] -= v[t] * wv + wv[t] * v
+        if vnext is not None:
+            tk, v = tnext, vnext
     d[n - 2], d[n - 1], e[n - 2] = rows[n - 2][n - 2], rows[n - 1][n - 1], rows[n - 1][n - 2]
     return d, e, tau, refl
 
