@@ -49,6 +49,16 @@ namespace gbxtb {
 
 namespace {
 
+// Storage of an FP64 pass's Householder reflectors (row k of A, right of the
+// diagonal): FP64 numbers, or double-float pairs (df64.cuh) when the on-chip
+// cluster kernel ran the pass in double-float arithmetic and the plan's
+// back-transformation is the one-warp kernel (at most 384 AOs), which then
+// applies them in double-float arithmetic too.  tau[n-1], which no reflector
+// uses, records it: kReflSplitFlag for pairs, 0 for FP64 numbers.
+constexpr double kReflSplitFlag = 1.0;
+// largest plan (AOs) whose back-transformation runs one warp per eigenvector
+constexpr int kBtWarpMaxN = 384;
+
 constexpr double kEps = 2.220446049250313e-16;
 constexpr double kSafeMin = 2.2250738585072014e-308;
 
@@ -457,6 +467,7 @@ __global__ void __launch_bounds__(kTrdThreads) k_tridiag(DevPlan pl, Work w) {
   if (w.prec[m] == 0 || cluster_pass(w.prec[m], md.nao)) return;
   extern __shared__ double sm[];
   __shared__ double red[32];
+  if (threadIdx.x == 0) w.tau[md.ao0 + md.nao - 1] = 0.0;  // reflectors as FP64 numbers
   tridiag_body<double>(md, w, sm, red);
 }
 
@@ -783,6 +794,7 @@ struct ClOpsNative {
   static __device__ __forceinline__ R load(G x) { return x; }
   static __device__ __forceinline__ G store(R x) { return x; }
   static __device__ __forceinline__ double to_d(R x) { return (double)x; }
+  static __device__ __forceinline__ R from_d(double x) { return (R)x; }
   static __device__ __forceinline__ bool is_zero(R x) { return x == R(0); }
   static __device__ __forceinline__ R add(R a, R b) { return a + b; }
   static __device__ __forceinline__ R mul(R a, R b) { return a * b; }
@@ -821,6 +833,7 @@ struct ClOps<df64> {
   static __device__ __forceinline__ df64 load(G x) { return df_from_double(x); }
   static __device__ __forceinline__ G store(df64 x) { return df_to_double(x); }
   static __device__ __forceinline__ double to_d(df64 x) { return df_to_double(x); }
+  static __device__ __forceinline__ df64 from_d(double x) { return df_from_double(x); }
   static __device__ __forceinline__ bool is_zero(df64 x) { return x.hi == 0.f; }
   static __device__ __forceinline__ df64 add(df64 a, df64 b) { return df_add(a, b); }
   static __device__ __forceinline__ df64 mul(df64 a, df64 b) { return df_mul(a, b); }
@@ -884,10 +897,12 @@ __device__ __forceinline__ T warp_sum4(T a0, T a1, T a2, T a3) {
 template <typename T>
 __device__ __forceinline__ void tridiag_cluster_onchip(cg::cluster_group &cluster, const MolDesc &md,
                                                        const Work &w, T *sm, T (*nrmw)[kClWarps],
-                                                       T (*kpw)[kClWarps], T *scal) {
+                                                       T (*kpw)[kClWarps], T *scal, bool refl_split) {
   using O = ClOps<T>;
   using G = typename O::G;
   using Acc = typename O::Acc;
+  // double-float reflectors stay pairs in A (kReflSplitFlag)
+  const bool split_store = std::is_same<T, df64>::value && refl_split;
   // FP32: every warp forms the scalars it needs itself (no CTA barrier);
   // FP64 and double-float: warp 0 alone (the FP64 pipe is scarce)
   constexpr bool kOneWarp = !std::is_same<T, float>::value;
@@ -951,6 +966,7 @@ __device__ __forceinline__ void tridiag_cluster_onchip(cg::cluster_group &cluste
     T *dst = rows + (size_t)li * n;
     for (int j = lane; j < n; j += 32) dst[j] = O::load(src[j]);
   }
+  if (rank == 0 && threadIdx.x == 0) tau[n - 1] = split_store ? kReflSplitFlag : 0.0;
   cluster.sync();
   if (n < 3) {
     if (threadIdx.x == 0) {
@@ -982,8 +998,13 @@ __device__ __forceinline__ void tridiag_cluster_onchip(cg::cluster_group &cluste
     T *ps = psb + (size_t)buf * nloc_max;
     T *colbuf = colb + (size_t)buf * nloc_max;
     const int lfirst = first_local(k + 1);
-    if (rank == 0)
-      for (int t = threadIdx.x; t < m1; t += blockDim.x) Ag[(int64_t)k * n + k + 1 + t] = O::store(vs[t]);
+    if (rank == 0) {
+      if (split_store)
+        for (int t = threadIdx.x; t < m1; t += blockDim.x)
+          reinterpret_cast<T *>(Ag)[(int64_t)k * n + k + 1 + t] = vs[t];
+      else
+        for (int t = threadIdx.x; t < m1; t += blockDim.x) Ag[(int64_t)k * n + k + 1 + t] = O::store(vs[t]);
+    }
     if (threadIdx.x == 32 && k > 0 && rank == k % kClusterSize) d[k] = O::to_d(own(k, k));
     // (1) p_k = tau A22 v for own rows (warp w takes the local rows li = w mod
     // nw, four at a time; the same rows it updates below), per-warp partial p.v
@@ -1086,7 +1107,7 @@ __host__ __device__ constexpr size_t onchip_smem_bytes(int n) {
 constexpr size_t kOnchipSmallBytes = 110 * 1024;
 
 __global__ void __cluster_dims__(kClusterSize, 1, 1) __launch_bounds__(kTrdClThreads)
-    k_tridiag_cluster(DevPlan pl, Work w, const int32_t *mol_list, int tail, int big, int df64_passes) {
+    k_tridiag_cluster(DevPlan pl, Work w, const int32_t *mol_list, int tail, int big, int df64_mode) {
   cg::cluster_group cluster = cg::this_cluster();
   const int m = list_mol(w, mol_list, blockIdx.x / kClusterSize);
   if (m < 0) return;  // the whole cluster
@@ -1103,16 +1124,19 @@ __global__ void __cluster_dims__(kClusterSize, 1, 1) __launch_bounds__(kTrdClThr
   const bool other_launch = big ? need <= kOnchipSmallBytes : need > kOnchipSmallBytes;
   const bool done = (w.phase[m] == kPhaseDone) || smem32 || md.nao > kClusterBlockedMinN || other_launch;
   if (!done) {
-    if (w.prec[m] && df64_passes)
+    // df64_mode: 0 native FP64; 1 double-float, reflectors stored as FP64;
+    // 2 double-float, reflectors stored as pairs
+    if (w.prec[m] && df64_mode)
       tridiag_cluster_onchip<df64>(cluster, md, w, reinterpret_cast<df64 *>(sm),
                                    reinterpret_cast<df64(*)[kClWarps]>(nrmw),
-                                   reinterpret_cast<df64(*)[kClWarps]>(kpw), reinterpret_cast<df64 *>(scal));
+                                   reinterpret_cast<df64(*)[kClWarps]>(kpw), reinterpret_cast<df64 *>(scal),
+                                   df64_mode == 2);
     else if (w.prec[m])
-      tridiag_cluster_onchip<double>(cluster, md, w, sm, nrmw, kpw, scal);
+      tridiag_cluster_onchip<double>(cluster, md, w, sm, nrmw, kpw, scal, false);
     else
       tridiag_cluster_onchip<float>(cluster, md, w, reinterpret_cast<float *>(sm),
                                     reinterpret_cast<float(*)[kClWarps]>(nrmw),
-                                    reinterpret_cast<float(*)[kClWarps]>(kpw), reinterpret_cast<float *>(scal));
+                                    reinterpret_cast<float(*)[kClWarps]>(kpw), reinterpret_cast<float *>(scal), false);
   }
   // no CTA leaves while others may still read its shared memory
   cluster.sync();
@@ -2038,21 +2062,23 @@ __global__ void __launch_bounds__(kBtThreads) k_backtransform(DevPlan pl, Work w
 template <typename T, int NQ, int QS>
 __device__ __forceinline__ void bt_apply_range(T (&y)[NQ], const T *A, const double *tau, int n, int lane,
                                                int khi, int klo) {
+  using O = ClOps<T>;
   for (int k = khi; k >= klo; --k) {
-    const T tk = (T)tau[k];
-    if (tk == T(0)) continue;
+    const double tk64 = tau[k];
+    if (tk64 == 0.0) continue;
+    const T tk = O::from_d(tk64);
     const T *v = A + (int64_t)k * n;  // reflector k: v[r] = A[k][r] multiplies row r > k
     T vq[NQ - QS];
-    T dot = T(0);
+    typename O::Acc acc = O::acc0();
 #pragma unroll
     for (int q = QS; q < NQ; ++q) {
       const int r = lane + 32 * q;
-      vq[q - QS] = (r > k && r < n) ? v[r] : T(0);
-      dot += vq[q - QS] * y[q];
+      vq[q - QS] = (r > k && r < n) ? v[r] : O::zero();
+      O::dot(acc, vq[q - QS], y[q]);
     }
-    dot = warp_sum(dot) * tk;
+    const T dot = O::mul(cl_warp_sum(O::fin(acc)), tk);
 #pragma unroll
-    for (int q = QS; q < NQ; ++q) y[q] -= dot * vq[q - QS];
+    for (int q = QS; q < NQ; ++q) y[q] = O::axpy_neg(y[q], dot, vq[q - QS]);
   }
 }
 
@@ -2066,24 +2092,29 @@ __device__ __forceinline__ void bt_apply_from(T (&y)[NQ], const T *A, const doub
   if constexpr (QS > 0) bt_apply_from<T, NQ, QS - 1>(y, A, tau, n, lane, kstart);
 }
 
+// T: the arithmetic (float in FP32 passes; double, or df64 where the
+// reflectors are double-float pairs, in FP64 passes); the eigenvector
+// matrix is FP32 or FP64 in memory (ClOps<T>::G)
 template <typename T, int NQ>
 __device__ __forceinline__ void backtransform_column(const MolDesc &md, const Work &w, int c) {
+  using O = ClOps<T>;
+  using G = typename O::G;
   const int n = md.nao;
   const int lane = threadIdx.x & 31;
-  const T *A = mat_view<T>(w.A, md.mat0);
+  const T *A = reinterpret_cast<const T *>(mat_view<G>(w.A, md.mat0));
   const double *tau = w.tau + md.ao0;
-  T *Y = mat_view<T>(w.Z, md.mat0);
+  G *Y = mat_view<G>(w.Z, md.mat0);
   T y[NQ];
 #pragma unroll
   for (int q = 0; q < NQ; ++q) {
     const int r = lane + 32 * q;
-    y[q] = (r < n) ? Y[(int64_t)r * n + c] : T(0);
+    y[q] = (r < n) ? O::load(Y[(int64_t)r * n + c]) : O::zero();
   }
   bt_apply_from<T, NQ, NQ - 1>(y, A, tau, n, lane, n - 3);
 #pragma unroll
   for (int q = 0; q < NQ; ++q) {
     const int r = lane + 32 * q;
-    if (r < n) Y[(int64_t)r * n + c] = y[q];
+    if (r < n) Y[(int64_t)r * n + c] = O::store(y[q]);
   }
 }
 
@@ -2098,7 +2129,9 @@ __global__ void __launch_bounds__(256, 2) k_backtransform_warp(DevPlan pl, Work 
   const int kvec = min(max(w.kvec[m], 0), md.nao);
   const int c = blockIdx.x * 8 + (threadIdx.x >> 5);
   if (c >= kvec) return;  // whole warp
-  if (w.prec[m])
+  if (w.prec[m] && w.tau[md.ao0 + md.nao - 1] == kReflSplitFlag)
+    backtransform_column<df64, NQ>(md, w, c);
+  else if (w.prec[m])
     backtransform_column<double, NQ>(md, w, c);
   else
     backtransform_column<float, NQ>(md, w, c);
@@ -2158,7 +2191,9 @@ int launch_tridiag_cluster(const DevPlan &pl, const Work &w, const int32_t *mol_
   // two size classes of shared memory (kOnchipSmallBytes)
   const size_t need = onchip_smem_bytes<double>(min(maxn, kClusterBlockedMinN));
   const size_t small = need < kOnchipSmallBytes ? need : kOnchipSmallBytes;
-  const int t = tail ? 1 : 0, sp = df64_passes ? 1 : 0;
+  // double-float reflectors stay pairs when the one-warp back-transformation
+  // (plans of at most 384 AOs) applies them
+  const int t = tail ? 1 : 0, sp = df64_passes ? (maxn <= kBtWarpMaxN ? 2 : 1) : 0;
   k_tridiag_cluster<<<count * kClusterSize, kTrdClThreads, small, s>>>(pl, w, mol_list, t, 0, sp);
   int launches = 1;
   if (need > kOnchipSmallBytes) {
@@ -2195,7 +2230,7 @@ void launch_invit(const DevPlan &pl, const Work &w, int maxn, cudaStream_t s) {
 void launch_backtransform(const DevPlan &pl, const Work &w, int maxn, const int32_t *mol_list, int count,
                           cudaStream_t s) {
   if (count <= 0) return;
-  if (maxn <= 384) {
+  if (maxn <= kBtWarpMaxN) {
     dim3 grid((maxn + 7) / 8, count);
     if (maxn <= 128)
       k_backtransform_warp<4><<<grid, 256, 0, s>>>(pl, w, mol_list);
