@@ -14,14 +14,21 @@
 //     FP64 GEMM kernel (64x64 tiles, 4x4 register micro-tiles) over a flat
 //     grid of (molecule, tile) pairs, skipping tiles outside triangular
 //     factors and computing symmetric products as lower tiles plus mirror;
-//   * tridiagonalisation: Householder, one block per molecule, warp-per-row
-//     symmetric matrix-vector products (coalesced rows);
-//   * eigenvalues: Sturm-sequence bisection, one thread per eigenvalue;
+//   * tridiagonalisation: Householder, by size and precision one CTA per
+//     molecule (FP32 in shared memory; FP64 up to 128 AOs), an 8-SM
+//     cluster with the matrix in the cluster's shared memory (up to 400
+//     AOs), or a blocked (panel) cluster kernel above;
+//   * eigenvalues: Sturm-sequence multisection, eight lanes per eigenvalue,
+//     FP64 Newton polish in FP64 passes;
 //   * eigenvectors: inverse iteration on the tridiagonal matrix, one thread
-//     per cluster of close eigenvalues (modified Gram-Schmidt inside a
-//     cluster), only for orbitals with non-zero Fermi occupation;
-//   * back-transformation: each thread owns one eigenvector column and
-//     applies all Householder reflectors to it.
+//     per eigenvector (modified Gram-Schmidt inside clusters of close
+//     eigenvalues), only for orbitals with non-zero Fermi occupation;
+//   * back-transformation: one warp per eigenvector column with the column
+//     in registers (above 384 AOs, blocks of columns with the reflector in
+//     shared memory).
+// In FP64 passes the on-chip cluster tridiagonalisation and its
+// back-transformation compute in double-float pairs on the FP32 pipe
+// (df64.cuh) in mixed-precision runs.
 //
 // Mixed precision.  GB300 retires 64 FP32 FMAs for every FP64 FMA, so the
 // early SCF passes of a molecule (potential change above ~1e-5) run the
@@ -747,31 +754,33 @@ __device__ __forceinline__ T ld_cg(const T *p) {
 // shared memory for the whole tridiagonalisation, so that the matrix-vector
 // product and the rank-2 update of a step touch only local shared memory.
 //
+// One exchange per step (one cluster barrier).  Step k starts with v_k in
+// every CTA and the CTA's rows updated through step k-1:
+//   (1) p_k = tau A22 v_k for its own rows: a warp takes four of its rows at
+//       a time and sums their four dot products over the lanes together
+//       (six adds by a transposed butterfly instead of twenty); p_k and the
+//       per-warp partials of p.v are published;
+//   (2) a copy of column k+1 of its rows, as it is before this step's
+//       update, is published;  -- cluster barrier --
+//   (3) every CTA gathers p and forms w_k = p - tau/2 (p.v) v for all rows;
+//   (4) every CTA applies this step's update to the gathered copy of column
+//       k+1 (the owners' expression, so bitwise their values), and
+//   (5) the owners apply A22 -= v w^T + w v^T to their rows (two FMAs per
+//       element), while
+//   (6) every CTA forms reflector k+1 from that column: its squared norm by
+//       a fixed-order block reduction, so tau and the scale are bitwise the
+//       same everywhere and every branch on them is uniform over the
+//       cluster.  A column with nothing to reduce gives tau = 0 and
+//       v = e_1, an exact identity update, so every step passes the same
+//       barriers.
+// Publications are double-buffered by the parity of k: a CTA rewrites a
+// buffer only after the barrier that follows every other CTA's last read.
 // The FP64 pipe of this GPU retires two FMAs per clock per SM (1/64 of the
 // FP32 rate), and an FP64 warp instruction holds it for 16 clocks whatever
-// its active lanes; a step is therefore laid out to issue as few FP64 warp
-// instructions as it can, more than to save latency:
-//   (a) warp 0 sums the 64 per-warp partial norms of column k (8 CTAs x 8
-//       warps), reads alpha from the owner of row k+1 and forms the
-//       reflector's scalars, which the other warps take from shared memory
-//       (one warp, not eight, runs the square root and the divisions);
-//       -- CTA barrier --  the CTA builds v from the owners' column
-//       entries (distributed shared memory);  -- CTA barrier --
-//   (b) p = tau A22 v for its own rows: a warp takes four rows at a time
-//       and sums their four dot products over the lanes together (six FP64
-//       adds by a transposed butterfly instead of twenty); per-warp
-//       partials of p.v are published;  -- cluster barrier 1 --
-//   (c) warp 0 sums the 64 partials of p.v;  -- CTA barrier --  the CTA
-//       gathers p from the owners and forms w = p - tau/2 (p.v) v;
-//       -- CTA barrier --
-//   (d) A22 -= v w^T + w v^T on its own rows (two FMAs per element), with
-//       the per-warp partial norm of column k+1 accumulated on the fly and
-//       published.  -- cluster barrier 2 --
-// Every CTA sums the same 64 partials in the same order (a fixed lane
-// assignment and butterfly), so tau, beta, the scale and w are bitwise the
-// same everywhere and every branch on them is uniform over the cluster.
-// Partials are double-buffered by the parity of k: a buffer is rewritten
-// only after a barrier that follows its last read.
+// its active lanes: in FP64 and double-float, warp 0 alone forms the
+// reflector's scalars and sums the cluster partials, which the other warps
+// read from shared memory after a CTA barrier; in FP32 every warp forms
+// them itself.
 // Output conventions as tridiag_body (reflector k in row k of A in global
 // memory, d, e, tau).
 constexpr int kClWarps = kTrdClThreads / 32;  // warps per CTA of the cluster kernels
