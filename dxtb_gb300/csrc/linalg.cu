@@ -1729,27 +1729,37 @@ __device__ __forceinline__ void bisect_body(const MolDesc &md, const Work &w, in
       hi = nhi;
     }
     if (r != 0) continue;
-    double x = 0.5 * ((double)lo + (double)hi);
-    if (kFp64) {
-      const double tol = 4.0 * Num<double>::eps * tnorm;
-      for (int it = 0; it < 6; ++it) {
-        const double dx = newton_correction(ds, e2, n, x);
-        x += dx;
-        if (!(fabs(dx) > tol)) break;
+    ev[idx] = 0.5 * ((double)lo + (double)hi);
+  }
+  if (!kFp64) return;
+  // FP64 pass: Newton polish of every start value of this block, one
+  // eigenvalue per thread (all lanes busy: an FP64 warp instruction holds
+  // the FP64 pipe for 16 clocks whatever its active lanes), after the
+  // start values of the whole block are written
+  __syncthreads();
+  const double tol = 4.0 * Num<double>::eps * tnorm;
+  const double delta = 64.0 * Num<double>::eps * tnorm + 1e-300;
+  for (int l = threadIdx.x;; l += blockDim.x) {
+    // the block's indices in the order of the loop above
+    const int idx = part * per_block + (l % per_block) + (l / per_block) * stride;
+    if (idx >= ncut || idx >= n) break;
+    double x = ev[idx];
+    for (int it = 0; it < 6; ++it) {
+      const double dx = newton_correction(ds, e2, n, x);
+      x += dx;
+      if (!(fabs(dx) > tol)) break;
+    }
+    const bool ok = isfinite(x) && sturm_count(ds, e2, n, x - delta, piv64) <= idx &&
+                    sturm_count(ds, e2, n, x + delta, piv64) > idx;
+    if (!ok) {
+      double blo = glo - 2.0 * Num<double>::eps * tnorm * n - 1e-300;
+      double bhi = fmax(cut, ghi) + 2.0 * Num<double>::eps * tnorm * n + 1e-300;
+      for (int it = 0; it < 128; ++it) {
+        const double mid = 0.5 * (blo + bhi);
+        if (mid <= blo || mid >= bhi) break;
+        if (sturm_count(ds, e2, n, mid, piv64) <= idx) blo = mid; else bhi = mid;
       }
-      const double delta = 64.0 * Num<double>::eps * tnorm + 1e-300;
-      const bool ok = isfinite(x) && sturm_count(ds, e2, n, x - delta, piv64) <= idx &&
-                      sturm_count(ds, e2, n, x + delta, piv64) > idx;
-      if (!ok) {
-        double blo = glo - 2.0 * Num<double>::eps * tnorm * n - 1e-300;
-        double bhi = fmax(cut, ghi) + 2.0 * Num<double>::eps * tnorm * n + 1e-300;
-        for (int it = 0; it < 128; ++it) {
-          const double mid = 0.5 * (blo + bhi);
-          if (mid <= blo || mid >= bhi) break;
-          if (sturm_count(ds, e2, n, mid, piv64) <= idx) blo = mid; else bhi = mid;
-        }
-        x = 0.5 * (blo + bhi);
-      }
+      x = 0.5 * (blo + bhi);
     }
     ev[idx] = x;
   }
