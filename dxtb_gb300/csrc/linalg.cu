@@ -1543,7 +1543,8 @@ __device__ __forceinline__ int sturm_count(const double *ds, const double *e2, i
     double pn = fma(ds[j] - x, pc, -e2[j - 1] * pm);
     const long long bits = __double_as_longlong(pn);
     const long long bc = __double_as_longlong(pc);
-    if (pn == 0.0) pn = (bc < 0) ? pivmin : -pivmin;
+    // zero test on the bits (an integer instruction, not an FP64 compare)
+    if ((bits << 1) == 0) pn = (bc < 0) ? pivmin : -pivmin;
     const long long bn = __double_as_longlong(pn);
     cnt += (int)((unsigned long long)(bn ^ bc) >> 63);
     const int ex = (int)((bits >> 52) & 0x7ff);
@@ -1599,6 +1600,10 @@ __device__ __forceinline__ int sturm_count(const float *ds, const float *e2, int
 
 constexpr int kBisectGroup = 8;  // lanes per eigenvalue in the multisection
 
+__device__ __forceinline__ unsigned long long dbits(double x) { return (unsigned long long)__double_as_longlong(x); }
+// biased binary exponent field of x (0 for zero and subnormals)
+__device__ __forceinline__ int dexp(double x) { return (int)((dbits(x) >> 52) & 0x7ff); }
+
 // Newton correction -p_n(x) / p_n'(x) of the characteristic polynomial
 // p_n(x) = det(T - x I) of the tridiagonal (ds, e2 = e^2):
 //   p_{j+1} = (d_j - x) p_j - e_{j-1}^2 p_{j-1},
@@ -1615,11 +1620,12 @@ __device__ __forceinline__ double newton_correction(const double *ds, const doub
     pc = pn;
     qm = qc;
     qc = qn;
-    const double mag = fmax(fmax(fabs(pc), fabs(qc)), fmax(fabs(pm), fabs(qm)));
-    const int ex = (int)((__double_as_longlong(mag) >> 52) & 0x7ff);
+    // largest binary exponent of the four running values, from their bits
+    // (integer instructions; FP64 max/abs would hold the FP64 pipe)
+    const int ex = max(max(dexp(pc), dexp(qc)), max(dexp(pm), dexp(qm)));
     if (ex > 1023 + 400) {
       pm *= 0x1p-400; pc *= 0x1p-400; qm *= 0x1p-400; qc *= 0x1p-400;
-    } else if (ex < 1023 - 400 && mag != 0.0) {
+    } else if (ex < 1023 - 400 && ((dbits(pc) | dbits(qc) | dbits(pm) | dbits(qm)) << 1) != 0) {
       pm *= 0x1p+400; pc *= 0x1p+400; qm *= 0x1p+400; qc *= 0x1p+400;
     }
   }
