@@ -1810,6 +1810,13 @@ constexpr int kInvitThreads = 256;
 // one inverse-iteration solve.  U1 holds the reciprocals of the pivots, so
 // that each element costs one division in the factorisation and none in the
 // two solves (a division is ~10 FP64 instructions).
+// |a| >= |b|: in FP64 from the bits (an integer compare; an FP64 compare
+// holds the FP64 pipe), the same result for every non-NaN pair
+template <typename T>
+__device__ __forceinline__ bool mag_ge(T a, T b) { return fabs(a) >= fabs(b); }
+template <>
+__device__ __forceinline__ bool mag_ge<double>(double a, double b) { return (dbits(a) << 1) >= (dbits(b) << 1); }
+
 template <typename T>
 __device__ __forceinline__ void invit_factor(int n, int i, T lam, const T *d, const T *e, T pert, T *U1,
                                              T *U2, T *U3, T *LM, T *PV) {
@@ -1820,8 +1827,8 @@ __device__ __forceinline__ void invit_factor(int n, int i, T lam, const T *d, co
     const T dn = d[j + 1] - lam;
     const T sup2 = (j + 1 < n - 1) ? e[j + 1] : T(0);
     const int64_t o = (int64_t)j * n + i;
-    if (fabs(u1) >= fabs(sub)) {
-      const bool tiny = fabs(u1) < pert;
+    if (mag_ge(u1, sub)) {
+      const bool tiny = !mag_ge(u1, pert);
       const T rinv = T(1) / (tiny ? ((u1 < T(0)) ? -pert : pert) : u1);
       const T mult = (u1 == T(0)) ? T(0) : (tiny ? sub / u1 : sub * rinv);
       U1[o] = rinv;
@@ -1844,7 +1851,7 @@ __device__ __forceinline__ void invit_factor(int n, int i, T lam, const T *d, co
     }
   }
   const int64_t o = (int64_t)(n - 1) * n + i;
-  U1[o] = T(1) / ((fabs(u1) < pert) ? ((u1 < T(0)) ? -pert : pert) : u1);
+  U1[o] = T(1) / (!mag_ge(u1, pert) ? ((u1 < T(0)) ? -pert : pert) : u1);
   U2[o] = T(0);
   U3[o] = T(0);
 }
