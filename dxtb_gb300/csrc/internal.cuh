@@ -43,8 +43,10 @@ constexpr int kClusterMinN = 128;
 constexpr int kClusterBlockedMinN = 400;
 // In the tail of a batch (fewer molecules than SMs), FP32 passes of
 // molecules with more AOs than this tridiagonalise on an 8-SM cluster with
-// the matrix in the cluster's shared memory instead of on one SM.
-constexpr int kTailClusterMinN = 160;
+// the matrix in the cluster's shared memory instead of on one SM (120
+// measured best with the one-exchange cluster step: 2.62 s per
+// 512-molecule call against 2.73 s at 160).
+constexpr int kTailClusterMinN = 120;
 
 // Passes that tridiagonalise on an 8-SM cluster in every pass (not only in
 // the tail of a batch): FP64 passes above kClusterMinN AOs and FP32 passes
