@@ -139,10 +139,12 @@ typedef struct {
                               own SCF where the faster mixer does not converge;
                               0: never */
   int32_t fp64_split;      /* arithmetic of the FP64 passes of the on-chip cluster
-                              tridiagonalisation (molecules of kClusterMinN < n
-                              <= 400 AOs): 0 (auto): double-float pairs on the
-                              FP32 pipe (~48 bits) with mixed_precision, native
-                              FP64 without; 1: native FP64; 2: double-float */
+                              tridiagonalisation (molecules of 129-400 AOs, and
+                              of up to 400 AOs once fewer molecules than SMs
+                              iterate) and of their back-transformation: 0 (auto):
+                              double-float pairs on the FP32 pipe (~48 bits)
+                              with mixed_precision, native FP64 without;
+                              1: native FP64; 2: double-float */
 } gbxtb_options;
 
 /* The reference's default SCF options (calculators/config/scf.py:139-190,
